@@ -1,0 +1,246 @@
+"""GB300-native QR hot path of CANDMC: TSQR, Householder reconstruction, CAQR.
+
+Python mirror of the reference's QR entry points (include/CANDMC.h ->
+alg/QR/tsqr/bitree_tsqr.h, alg/QR/hh_recon/hh_recon.h, alg/QR/qr_2d/qr_2d.h)
+on one GPU: the process grid is 1 x 1, so the MPI arguments (myRank, numPes,
+root, req_id, CommData_t, pview) disappear.  Every function calls the C ABI
+of libcandmc_gb300.so (include/candmc_gb300.h); there is no CPU fallback and
+an unbuilt library raises.
+
+Matrices are column-major float64, as in the reference:
+  * device arrays: torch CUDA tensors with stride(0) == 1 (see `colmajor`),
+    the leading dimension is stride(1); work is enqueued on the current torch
+    stream (or `stream`);
+  * host arrays: numpy float64 in Fortran order, updated in place (the
+    reference's pointers are host memory).
+Errors raise CandmcError (the reference asserts/aborts instead).
+"""
+import numpy as np
+
+from . import _abi
+from ._abi import CandmcError, check
+
+__all__ = [
+    "CandmcError", "colmajor", "empty_colmajor", "hh_recon_qr", "bitree_tsqr", "construct_Q1",
+    "compute_invT_from_W", "signed_NLU", "recursive_NLU", "compute_invT_from_Y",
+    "compute_invT_from_Y2", "upd_A", "update_A", "QR_2D", "QR_2D_2D", "QR_2D_pipe",
+    "PRECISIONS", "lib",
+]
+
+PRECISIONS = {"fp64": 0, "ozaki": 1, "fp32": 2}
+
+
+def lib():
+    return _abi.load()
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def colmajor(x):
+    """Column-major copy of a 2-D torch tensor (stride(0) == 1)."""
+    return x.t().contiguous().t()
+
+
+def empty_colmajor(m, n, device="cuda", dtype=None):
+    torch = _torch()
+    return torch.empty((n, m), dtype=dtype or torch.float64, device=device).t()
+
+
+def _is_torch(x):
+    try:
+        import torch
+    except ImportError:
+        return False
+    return isinstance(x, torch.Tensor)
+
+
+def _dev(x, name, rows=None):
+    """(pointer, leading dimension) of a column-major CUDA float64 tensor."""
+    torch = _torch()
+    if not (isinstance(x, torch.Tensor) and x.is_cuda):
+        raise TypeError(f"{name}: expected a CUDA tensor")
+    if x.dtype not in (torch.float64, torch.int64):
+        raise TypeError(f"{name}: expected float64")
+    if x.dim() == 1:
+        return x.data_ptr(), max(1, x.shape[0])
+    if x.stride(0) != 1 and x.shape[0] > 1:
+        raise ValueError(f"{name}: must be column-major (stride(0) == 1); use colmajor()")
+    ld = x.stride(1) if x.shape[1] > 1 else max(1, x.shape[0])
+    return x.data_ptr(), ld
+
+
+def _stream(stream):
+    if stream is None:
+        return _torch().cuda.current_stream().cuda_stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+def _host(x, name):
+    if not isinstance(x, np.ndarray) or x.dtype != np.float64 or not x.flags.f_contiguous:
+        raise TypeError(f"{name}: expected a Fortran-ordered float64 numpy array")
+    if not x.flags.writeable:
+        raise ValueError(f"{name}: must be writeable (updated in place)")
+    return x.ctypes.data, max(1, x.shape[0])
+
+
+def _prec(p):
+    if isinstance(p, str):
+        return PRECISIONS[p]
+    return int(p)
+
+
+# ------------------------------------------------------------------ panel
+def hh_recon_qr(A, W=None, T=None, stream=None):
+    """TSQR + Householder reconstruction (alg/QR/hh_recon/hh_recon.h:66-75).
+
+    A (m x b) is overwritten with Y\\(S*R).  Returns (W, T): W = U*S =
+    -T*Y1^T (b x b upper) and T, the compact-WY factor Q = I - Y T Y^T.
+    """
+    m, b = A.shape
+    if isinstance(A, np.ndarray):
+        pa, lda = _host(A, "A")
+        W = np.zeros((b, b), order="F") if W is None else W
+        T = np.zeros((b, b), order="F") if T is None else T
+        check(lib().candmc_hh_recon_qr_host(pa, lda, m, b, _host(W, "W")[0], _host(T, "T")[0]),
+              "hh_recon_qr")
+        return W, T
+    W = empty_colmajor(b, b, A.device) if W is None else W
+    T = empty_colmajor(b, b, A.device) if T is None else T
+    pa, lda = _dev(A, "A")
+    check(lib().candmc_hh_recon_qr(pa, lda, m, b, _dev(W, "W")[0], _dev(T, "T")[0], _stream(stream)),
+          "hh_recon_qr")
+    return W, T
+
+
+def bitree_tsqr(A, output_Y=1, stream=None):
+    """Single-rank binary-tree TSQR (alg/QR/tsqr/bitree_tsqr.h:58-70): returns (R, tau);
+    A becomes the LAPACK-form Y\\R when output_Y."""
+    m, b = A.shape
+    R = empty_colmajor(b, b, A.device)
+    tau = _torch().empty(b, dtype=_torch().float64, device=A.device)
+    pa, lda = _dev(A, "A")
+    check(lib().candmc_bitree_tsqr(pa, lda, _dev(R, "R")[0], tau.data_ptr(), m, b, int(output_Y),
+                                   _stream(stream)), "bitree_tsqr")
+    return R, tau
+
+
+def construct_Q1(Y, tau, k=None, stream=None):
+    """First k columns of the TSQR Q (alg/QR/tsqr/bitree_tsqr.h:91-104, numPes = 1)."""
+    m, b = Y.shape
+    k = b if k is None else k
+    Q1 = empty_colmajor(m, k, Y.device)
+    py, ldy = _dev(Y, "Y")
+    check(lib().candmc_construct_Q1(py, ldy, tau.data_ptr(), _dev(Q1, "Q1")[0], _dev(Q1, "Q1")[1],
+                                    m, b, k, _stream(stream)), "construct_Q1")
+    return Q1
+
+
+def compute_invT_from_W(W, Y1, stream=None):
+    """T^-T from W and Y1 (alg/QR/hh_recon/hh_recon.h:13-15): solves W^T X = -Y1."""
+    b = W.shape[0]
+    X = colmajor(Y1.clone())
+    check(lib().candmc_compute_invT_from_W(_dev(W, "W")[0], b, _dev(X, "invT")[0], _stream(stream)),
+          "compute_invT_from_W")
+    return X
+
+
+def _nlu(fn, A, R, stream):
+    b = A.shape[0]
+    signs = _torch().empty(b, dtype=_torch().int64, device=A.device)
+    pa, lda = _dev(A, "A")
+    pr, ldr = _dev(R, "R")
+    check(fn(pa, pr, b, lda, ldr, signs.data_ptr(), _stream(stream)), "NLU")
+    return signs
+
+
+def signed_NLU(A, R, stream=None):
+    """Sign-choice LU of (A - S) in place (alg/QR/hh_recon/hh_recon.h:27-36); returns signs."""
+    return _nlu(lib().candmc_signed_NLU, A, R, stream)
+
+
+def recursive_NLU(A, R, stream=None):
+    """Recursive signed LU (alg/QR/hh_recon/hh_recon.h:38-49); returns signs."""
+    return _nlu(lib().candmc_recursive_NLU, A, R, stream)
+
+
+# ------------------------------------------------------------------ T factor
+def compute_invT_from_Y(Y, T=None, stream=None):
+    """T^-T = stril(Y^T Y), halved diagonal (alg/QR/qr_2d/qr_2d.h:25-31).  Writes the lower part of T."""
+    mb, b = Y.shape
+    T = _torch().zeros((b, b), dtype=_torch().float64, device=Y.device).t() if T is None else T
+    py, ldy = _dev(Y, "Y")
+    pt, ldt = _dev(T, "T")
+    check(lib().candmc_compute_invT_from_Y(py, ldy, pt, ldt, mb, b, _stream(stream)), "compute_invT_from_Y")
+    return T
+
+
+def compute_invT_from_Y2(Y1, Y2, stream=None):
+    """Y1^T Y2 (alg/QR/qr_2d/qr_2d.h:47-56)."""
+    mb, b1 = Y1.shape
+    b2 = Y2.shape[1]
+    T = empty_colmajor(b1, b2, Y1.device)
+    p1, l1 = _dev(Y1, "Y1")
+    p2, l2 = _dev(Y2, "Y2")
+    pt, ldt = _dev(T, "T")
+    check(lib().candmc_compute_invT_from_Y2(p1, l1, p2, l2, pt, ldt, mb, b1, b2, _stream(stream)),
+          "compute_invT_from_Y2")
+    return T
+
+
+# ------------------------------------------------------------------ CAQR
+def upd_A(Y, A, W=None, W_is_T=False, precision="fp64", stream=None):
+    """A <- (I - Y T Y^T)^T A (alg/QR/qr_2d/qr_2d.h:99-108); Y explicit (unit diagonal stored)."""
+    mb, b = Y.shape
+    kb = A.shape[1]
+    py, ldy = _dev(Y, "Y")
+    pa, lda = _dev(A, "A")
+    pw = _dev(W, "W")[0] if W is not None else None
+    check(lib().candmc_upd_A(py, ldy, pa, lda, mb, kb, b, pw, int(bool(W_is_T)), _prec(precision),
+                             _stream(stream)), "upd_A")
+    return A
+
+
+def update_A(YR, A, b, W=None, aggreg_Y=None, W_is_T=False, precision="fp64", stream=None):
+    """update_A (alg/QR/qr_2d/qr_2d.h:74-85): Y read from the Y\\R buffer YR (m x b)."""
+    m, k = A.shape
+    py, ldy = _dev(YR, "YR")
+    pa, lda = _dev(A, "A")
+    pw = _dev(W, "W")[0] if W is not None else None
+    pg, ldg = _dev(aggreg_Y, "aggreg_Y") if aggreg_Y is not None else (None, 0)
+    check(lib().candmc_update_A(py, ldy, pa, lda, m, k, b, pw, pg, ldg, int(bool(W_is_T)),
+                                _prec(precision), _stream(stream)), "update_A")
+    return A
+
+
+def QR_2D(A, b, aggreg_Y=None, precision="fp64", stream=None):
+    """Right-looking CAQR (alg/QR/qr_2d/qr_2d.h:124-131) on a 1 x 1 grid; A becomes Y\\R."""
+    m, k = A.shape
+    if isinstance(A, np.ndarray):
+        pa, lda = _host(A, "A")
+        check(lib().candmc_QR_2D_host(pa, lda, m, k, b, _prec(precision)), "QR_2D")
+        return A
+    pa, lda = _dev(A, "A")
+    pg, ldg = _dev(aggreg_Y, "aggreg_Y") if aggreg_Y is not None else (None, 0)
+    check(lib().candmc_QR_2D(pa, lda, m, k, b, pg, ldg, _prec(precision), _stream(stream)), "QR_2D")
+    return A
+
+
+def QR_2D_2D(A, b, b_sub, aggreg_Y=None, precision="fp64", stream=None):
+    """Two-level blocked CAQR (alg/QR/qr_2d/qr_2d.h:176-188)."""
+    m, k = A.shape
+    pa, lda = _dev(A, "A")
+    pg, ldg = _dev(aggreg_Y, "aggreg_Y") if aggreg_Y is not None else (None, 0)
+    check(lib().candmc_QR_2D_2D(pa, lda, m, k, b, b_sub, pg, ldg, _prec(precision), _stream(stream)),
+          "QR_2D_2D")
+    return A
+
+
+def QR_2D_pipe(A, b, precision="fp64", stream=None):
+    """Lookahead CAQR (alg/QR/qr_2d/qr_2d.h:293-302): the same factorization on one GPU."""
+    m, k = A.shape
+    pa, lda = _dev(A, "A")
+    check(lib().candmc_QR_2D_pipe(pa, lda, m, k, b, _prec(precision), _stream(stream)), "QR_2D_pipe")
+    return A

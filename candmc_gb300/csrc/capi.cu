@@ -1,0 +1,453 @@
+// C ABI and host orchestration of the QR hot path (include/candmc_gb300.h).
+//
+// hh_recon_qr is computed by recursive column blocking: a panel wider than
+// kDirectB is split in two halves; the left half is reconstructed, the right
+// half receives the left half's Q^T, the lower part of the right half is
+// reconstructed, and the two compact-WY factors are merged
+// (T12 = -T11 * Y1^T Y2 * T22, LAPACK dlarft's block form).  The blocked
+// Householder factor equals the unblocked one in exact arithmetic (it is
+// what LAPACK's blocked dgeqrf relies on), so the output is the same
+// canonical (Y, T, S*R) as the reference's single-panel reconstruction
+// (alg/QR/hh_recon/hh_recon.cxx:129-321), while the FP64 tree-node work stays
+// at 32-column nodes.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+
+#include "kernels.cuh"
+
+namespace candmc {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char* what) {
+  g_last_error = what ? what : "";
+  return code;
+}
+
+int cuda_status(cudaError_t e, const char* where) {
+  g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return CANDMC_ERR_ALLOC;
+  return CANDMC_ERR_CUDA;
+}
+
+int DevBuf::alloc(size_t bytes, cudaStream_t stream) {
+  s = stream;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMallocAsync(&p, bytes, stream);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    return cuda_status(e, "cudaMallocAsync");
+  }
+  return CANDMC_OK;
+}
+
+DevBuf::~DevBuf() {
+  if (p) cudaFreeAsync(p, s);
+}
+
+// C <- (I - Y T Y^T)^T C = C - Y * (T^T * (Y^T * C))
+int apply_qt(const double* Y, int64_t ldy, int64_t m, int nb, const double* T, int64_t ldT,
+             double* C, int64_t ldc, int64_t n, int precision, cudaStream_t s);
+
+// Recursive blocked TSQR-HR (see file comment).  T (ldT) receives the b x b
+// upper-triangular factor; the strictly lower part of T is zeroed.
+static int hr_rec(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, int* st,
+                  int precision, cudaStream_t s) {
+  if (b <= kDirectB) return hr_direct(A, lda, m, b, T, ldT, nullptr, 0, st, s);
+  const int b1 = b / 2, b2 = b - b1;
+  CANDMC_RET(hr_rec(A, lda, m, b1, T, ldT, st, precision, s));
+  CANDMC_RET(apply_qt(A, lda, m, b1, T, ldT, A + (int64_t)b1 * lda, lda, b2, precision, s));
+  double* T22 = T + (int64_t)b1 * ldT + b1;
+  CANDMC_RET(hr_rec(A + (int64_t)b1 * lda + b1, lda, m - b1, b2, T22, ldT, st, precision, s));
+  // G = Y1[b1:m, :]^T * Y2   (Y2 unit-lower in A[b1:, b1:])
+  DevBuf g, x;
+  CANDMC_RET(g.alloc(sizeof(double) * b1 * b2, s));
+  CANDMC_RET(x.alloc(sizeof(double) * b1 * b2, s));
+  CANDMC_RET(gemm_tn_reduce(mref(A + b1, lda), mref(A + (int64_t)b1 * lda + b1, lda, 0, kUnitLower),
+                            m - b1, b1, b2, mref(nullptr, 0), 1.0, g.d(), b1, s));
+  // X = T11 * G;  T12 = -X * T22
+  CANDMC_RET(small_gemm(b1, b2, b1, 1.0, mref(T, ldT, 0, kUpper), mref(g.d(), b1), 0.0, x.d(), b1, s));
+  CANDMC_RET(small_gemm(b1, b2, b2, -1.0, mref(x.d(), b1), mref(T22, ldT, 0, kUpper), 0.0,
+                        T + (int64_t)b1 * ldT, ldT, s));
+  CANDMC_CK(cudaMemset2DAsync(T + b1, sizeof(double) * ldT, 0, sizeof(double) * b2, b1, s));
+  return CANDMC_OK;
+}
+
+int apply_qt(const double* Y, int64_t ldy, int64_t m, int nb, const double* T, int64_t ldT,
+             double* C, int64_t ldc, int64_t n, int precision, cudaStream_t s) {
+  if (n <= 0 || m <= 0) return CANDMC_OK;
+  if (precision != CANDMC_PREC_FP64) return set_error(CANDMC_ERR_ARG, "precision form not built");
+  DevBuf z;
+  CANDMC_RET(z.alloc(sizeof(double) * (size_t)nb * n, s));
+  MatRef Ym = mref(Y, ldy, 0, kUnitLower);
+  CANDMC_RET(gemm_tn_reduce(Ym, mref(C, ldc), m, nb, n, mref(T, ldT, 1, kUpper), 1.0, z.d(), nb, s));
+  CANDMC_RET(gemm_nn_sub(C, ldc, Ym, z.d(), nb, m, n, nb, s));
+  return CANDMC_OK;
+}
+
+// Top-level TSQR-HR with optional W = -T * Y1^T (ld ldW) and T (ld ldT).
+static int hh_recon_dev(double* A, int64_t lda, int64_t m, int64_t b, double* W, int64_t ldW,
+                        double* T, int64_t ldT, int* st, int precision, cudaStream_t s) {
+  DevBuf tb;
+  if (!T) {
+    CANDMC_RET(tb.alloc(sizeof(double) * b * b, s));
+    T = tb.d();
+    ldT = b;
+  }
+  if (b <= kDirectB) return hr_direct(A, lda, m, (int)b, T, ldT, W, ldW, st, s);
+  CANDMC_RET(hr_rec(A, lda, m, (int)b, T, ldT, st, precision, s));
+  if (W) {
+    CANDMC_RET(small_gemm(b, b, b, -1.0, mref(T, ldT, 0, kUpper), mref(A, lda, 1, kUnitLower), 0.0,
+                          W, ldW, s));
+  }
+  return CANDMC_OK;
+}
+
+// Tᵀ-application factor for upd_A's W conventions (qr_2d.cxx:242-253):
+// returns Top (b x b lower, ld b) with Top = T^T.
+static int top_from_W(const double* Y, int64_t ldy, int64_t mb, int64_t b, const double* W,
+                      int W_is_T, int ymask, double* Top, cudaStream_t s) {
+  DevBuf x;
+  CANDMC_RET(x.alloc(sizeof(double) * b * b, s));
+  if (W == nullptr) {
+    // T^-T = stril(Y^T Y) with halved diagonal, T^T = (T^-T)^-1
+    CANDMC_RET(gemm_tn_reduce(mref(Y, ldy, 0, ymask), mref(Y, ldy, 0, ymask), mb, (int)b, b,
+                              mref(nullptr, 0), 1.0, x.d(), b, s));
+    CANDMC_CK(cudaMemsetAsync(Top, 0, sizeof(double) * b * b, s));
+    CANDMC_RET(invT_from_gram(x.d(), b, (int)b, Top, b, s));
+    CANDMC_CK(cudaMemcpyAsync(x.d(), Top, sizeof(double) * b * b, cudaMemcpyDeviceToDevice, s));
+    CANDMC_RET(tri_inv(x.d(), b, (int)b, 1, 0, Top, b, s));
+  } else if (W_is_T) {
+    CANDMC_RET(tri_inv(W, b, (int)b, 1, 0, Top, b, s));
+  } else {
+    // T^-T = -W^-T Y1  =>  T^T = -Y1^-1 W^T
+    CANDMC_RET(tri_inv(Y, ldy, (int)b, 1, 1, x.d(), b, s));
+    CANDMC_RET(small_gemm(b, b, b, -1.0, mref(x.d(), b, 0, kLower), mref(W, b, 1, kUpper), 0.0,
+                          Top, b, s));
+  }
+  return CANDMC_OK;
+}
+
+static int upd_core(const double* Y, int64_t ldy, int ymask, double* A, int64_t lda, int64_t mb,
+                    int64_t kb, int64_t b, const double* W, int W_is_T, int precision,
+                    cudaStream_t s) {
+  if (mb <= 0 || kb <= 0) return CANDMC_OK;
+  if (precision != CANDMC_PREC_FP64) return set_error(CANDMC_ERR_ARG, "precision form not built");
+  DevBuf top, z;
+  CANDMC_RET(top.alloc(sizeof(double) * b * b, s));
+  CANDMC_RET(z.alloc(sizeof(double) * b * kb, s));
+  CANDMC_RET(top_from_W(Y, ldy, mb, b, W, W_is_T, ymask, top.d(), s));
+  MatRef Ym = mref(Y, ldy, 0, ymask);
+  CANDMC_RET(gemm_tn_reduce(Ym, mref(A, lda), mb, (int)b, kb, mref(top.d(), b, 0, kLower), 1.0,
+                            z.d(), b, s));
+  CANDMC_RET(gemm_nn_sub(A, lda, Ym, z.d(), b, mb, kb, (int)b, s));
+  return CANDMC_OK;
+}
+
+static int qr_2d_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, double* aggreg_Y,
+                     int64_t lda_aY, int* st, int precision, cudaStream_t s) {
+  DevBuf tb;
+  CANDMC_RET(tb.alloc(sizeof(double) * b * b, s));
+  int64_t r0 = 0;
+  for (;;) {
+    const int64_t mm = m - r0, kk = k - r0;
+    const int64_t bb = std::min(kk, b);
+    double* P = A + r0 * lda + r0;
+    CANDMC_RET(hr_rec(P, lda, mm, (int)bb, tb.d(), b, st, precision, s));
+    if (aggreg_Y)
+      CANDMC_RET(materialize(mref(P, lda, 0, kUnitLower), mm, bb, aggreg_Y + r0 * lda_aY + r0,
+                             lda_aY, s));
+    if (kk - b > 0 && mm - b > 0) {
+      CANDMC_RET(apply_qt(P, lda, mm, (int)b, tb.d(), b, P + b * lda, lda, kk - b, precision, s));
+      r0 += b;
+    } else {
+      break;
+    }
+  }
+  return CANDMC_OK;
+}
+
+// Per-call device status word.
+struct Status {
+  DevBuf buf;
+  int init(cudaStream_t s) {
+    CANDMC_RET(buf.alloc(sizeof(int), s));
+    CANDMC_CK(cudaMemsetAsync(buf.p, 0, sizeof(int), s));
+    return CANDMC_OK;
+  }
+  int* p() { return static_cast<int*>(buf.p); }
+  int check(cudaStream_t s) {
+    int h = 0;
+    CANDMC_CK(cudaMemcpyAsync(&h, buf.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CANDMC_CK(cudaStreamSynchronize(s));
+    return h;
+  }
+};
+
+static int device_ok() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return set_error(CANDMC_ERR_NODEV, "no CUDA device");
+  return CANDMC_OK;
+}
+
+// Host staging helper: device copy of a column-major m x n block with leading dimension ld.
+struct HostMat {
+  DevBuf d;
+  int64_t ldd = 0;
+  int in(const double* h, int64_t ld, int64_t m, int64_t n, cudaStream_t s) {
+    ldd = std::max<int64_t>(m, 1);
+    CANDMC_RET(d.alloc(sizeof(double) * (size_t)ldd * std::max<int64_t>(n, 1), s));
+    if (m > 0 && n > 0)
+      CANDMC_CK(cudaMemcpy2DAsync(d.p, sizeof(double) * ldd, h, sizeof(double) * ld,
+                                  sizeof(double) * m, n, cudaMemcpyHostToDevice, s));
+    return CANDMC_OK;
+  }
+  int out(double* h, int64_t ld, int64_t m, int64_t n, cudaStream_t s) {
+    if (m > 0 && n > 0)
+      CANDMC_CK(cudaMemcpy2DAsync(h, sizeof(double) * ld, d.p, sizeof(double) * ldd,
+                                  sizeof(double) * m, n, cudaMemcpyDeviceToHost, s));
+    return CANDMC_OK;
+  }
+};
+
+}  // namespace candmc
+
+using namespace candmc;
+
+#define STREAM(x) static_cast<cudaStream_t>(x)
+
+extern "C" {
+
+const char* candmc_status_string(int status) {
+  switch (status) {
+    case CANDMC_OK: return "ok";
+    case CANDMC_ERR_ARG: return "invalid argument";
+    case CANDMC_ERR_ALLOC: return "allocation failed";
+    case CANDMC_ERR_CUDA: return "CUDA error";
+    case CANDMC_ERR_TIMEOUT: return "device wait timed out";
+    case CANDMC_ERR_NUMERIC: return "non-finite value or zero pivot";
+    case CANDMC_ERR_NODEV: return "no usable CUDA device";
+    default: return "unknown status";
+  }
+}
+
+int candmc_version(void) { return 100; }
+
+const char* candmc_last_error(void) { return g_last_error.c_str(); }
+
+int candmc_hh_recon_qr(double* A, int64_t lda, int64_t m, int64_t b, double* W, double* T,
+                       void* stream) {
+  if (!A || !W || b < 1 || m < b || lda < m) return set_error(CANDMC_ERR_ARG, "hh_recon_qr args");
+  cudaStream_t s = STREAM(stream);
+  Status st;
+  CANDMC_RET(st.init(s));
+  return hh_recon_dev(A, lda, m, b, W, b, T, b, st.p(), CANDMC_PREC_FP64, s);
+}
+
+int candmc_hh_recon_qr_host(double* A, int64_t lda, int64_t m, int64_t b, double* W, double* T) {
+  if (!A || !W || b < 1 || m < b || lda < m) return set_error(CANDMC_ERR_ARG, "hh_recon_qr args");
+  CANDMC_RET(device_ok());
+  cudaStream_t s = nullptr;
+  int rc;
+  {
+    HostMat dA;
+    DevBuf dW, dT;
+    Status st;
+    CANDMC_RET(st.init(s));
+    CANDMC_RET(dA.in(A, lda, m, b, s));
+    CANDMC_RET(dW.alloc(sizeof(double) * b * b, s));
+    CANDMC_RET(dT.alloc(sizeof(double) * b * b, s));
+    CANDMC_RET(hh_recon_dev(dA.d.d(), dA.ldd, m, b, dW.d(), b, dT.d(), b, st.p(), CANDMC_PREC_FP64, s));
+    CANDMC_RET(dA.out(A, lda, m, b, s));
+    CANDMC_CK(cudaMemcpyAsync(W, dW.p, sizeof(double) * b * b, cudaMemcpyDeviceToHost, s));
+    if (T) CANDMC_CK(cudaMemcpyAsync(T, dT.p, sizeof(double) * b * b, cudaMemcpyDeviceToHost, s));
+    rc = st.check(s);
+  }
+  CANDMC_CK(cudaStreamSynchronize(s));
+  return rc;
+}
+
+int candmc_bitree_tsqr(double* A, int64_t lda, double* R, double* tau, int64_t m, int64_t b,
+                       int output_Y, void* stream) {
+  if (!A || !R || !tau || b < 1 || m < b || lda < m) return set_error(CANDMC_ERR_ARG, "bitree_tsqr args");
+  cudaStream_t s = STREAM(stream);
+  Status st;
+  CANDMC_RET(st.init(s));
+  DevBuf tb, work;
+  CANDMC_RET(tb.alloc(sizeof(double) * b * b, s));
+  double* P = A;
+  int64_t ldp = lda;
+  if (!output_Y) {
+    CANDMC_RET(work.alloc(sizeof(double) * m * b, s));
+    CANDMC_CK(cudaMemcpy2DAsync(work.p, sizeof(double) * m, A, sizeof(double) * lda,
+                                sizeof(double) * m, b, cudaMemcpyDeviceToDevice, s));
+    P = work.d();
+    ldp = m;
+  }
+  CANDMC_RET(hh_recon_dev(P, ldp, m, b, nullptr, 0, tb.d(), b, st.p(), CANDMC_PREC_FP64, s));
+  CANDMC_RET(materialize(mref(P, ldp, 0, kUpper), b, b, R, b, s));
+  // tau_i = T_ii
+  CANDMC_CK(cudaMemcpy2DAsync(tau, sizeof(double), tb.p, sizeof(double) * (b + 1), sizeof(double),
+                              b, cudaMemcpyDeviceToDevice, s));
+  return CANDMC_OK;
+}
+
+int candmc_construct_Q1(const double* Y, int64_t ldy, const double* tau, double* Q1, int64_t ldq,
+                        int64_t m, int64_t b, int64_t k, void* stream) {
+  if (!Y || !tau || !Q1 || b < 1 || k < 1 || k > b || m < b || ldy < m || ldq < m)
+    return set_error(CANDMC_ERR_ARG, "construct_Q1 args");
+  cudaStream_t s = STREAM(stream);
+  DevBuf g, t, z;
+  CANDMC_RET(g.alloc(sizeof(double) * b * b, s));
+  CANDMC_RET(t.alloc(sizeof(double) * b * b, s));
+  CANDMC_RET(z.alloc(sizeof(double) * b * k, s));
+  MatRef Ym = mref(Y, ldy, 0, kUnitLower);
+  CANDMC_RET(gemm_tn_reduce(Ym, Ym, m, (int)b, b, mref(nullptr, 0), 1.0, g.d(), b, s));
+  CANDMC_RET(larft_from_gram(g.d(), b, tau, (int)b, t.d(), b, s));
+  // Z = T * Y[0:k, :]^T  (b x k);  Q1 = E - Y * Z
+  CANDMC_RET(small_gemm(b, k, b, 1.0, mref(t.d(), b, 0, kUpper), mref(Y, ldy, 1, kUnitLower), 0.0,
+                        z.d(), b, s));
+  CANDMC_RET(set_identity(Q1, ldq, m, k, s));
+  CANDMC_RET(gemm_nn_sub(Q1, ldq, Ym, z.d(), b, m, k, (int)b, s));
+  return CANDMC_OK;
+}
+
+int candmc_compute_invT_from_W(const double* W, int64_t b, double* invT, void* stream) {
+  if (!W || !invT || b < 1) return set_error(CANDMC_ERR_ARG, "compute_invT_from_W args");
+  cudaStream_t s = STREAM(stream);
+  DevBuf wi, y1;
+  CANDMC_RET(wi.alloc(sizeof(double) * b * b, s));
+  CANDMC_RET(y1.alloc(sizeof(double) * b * b, s));
+  CANDMC_CK(cudaMemcpyAsync(y1.p, invT, sizeof(double) * b * b, cudaMemcpyDeviceToDevice, s));
+  CANDMC_RET(tri_inv(W, b, (int)b, 0, 0, wi.d(), b, s));
+  // X = -W^-T * Y1
+  CANDMC_RET(small_gemm(b, b, b, -1.0, mref(wi.d(), b, 1, kUpper), mref(y1.d(), b), 0.0, invT, b, s));
+  return CANDMC_OK;
+}
+
+int candmc_signed_NLU(double* A, double* R, int64_t b, int64_t lda, int64_t ldr, int64_t* signs,
+                      void* stream) {
+  if (!A || !R || !signs || b < 1 || lda < b || ldr < b) return set_error(CANDMC_ERR_ARG, "NLU args");
+  return signed_nlu(A, R, b, lda, ldr, signs, STREAM(stream));
+}
+
+int candmc_recursive_NLU(double* A, double* R, int64_t b, int64_t lda, int64_t ldr,
+                         int64_t* signs, void* stream) {
+  // The recursion of hh_recon.cxx:80-110 reorders the same elimination; one
+  // kernel performs it directly.
+  return candmc_signed_NLU(A, R, b, lda, ldr, signs, stream);
+}
+
+int candmc_compute_invT_from_Y(const double* Y, int64_t ldy, double* T, int64_t ldt, int64_t mb,
+                               int64_t b, void* stream) {
+  if (!Y || !T || b < 1 || mb < 0 || ldt < b) return set_error(CANDMC_ERR_ARG, "invT_from_Y args");
+  cudaStream_t s = STREAM(stream);
+  DevBuf g;
+  CANDMC_RET(g.alloc(sizeof(double) * b * b, s));
+  if (mb > 0) {
+    CANDMC_RET(gemm_tn_reduce(mref(Y, ldy), mref(Y, ldy), mb, (int)b, b, mref(nullptr, 0), 1.0,
+                              g.d(), b, s));
+  } else {
+    CANDMC_CK(cudaMemsetAsync(g.p, 0, sizeof(double) * b * b, s));
+  }
+  return invT_from_gram(g.d(), b, (int)b, T, ldt, s);
+}
+
+int candmc_compute_invT_from_Y2(const double* Y1, int64_t ldy1, const double* Y2, int64_t ldy2,
+                                double* T, int64_t ldt, int64_t mb, int64_t b1, int64_t b2,
+                                void* stream) {
+  if (!Y1 || !Y2 || !T || b1 < 1 || b2 < 1 || ldt < b1) return set_error(CANDMC_ERR_ARG, "invT_from_Y2 args");
+  cudaStream_t s = STREAM(stream);
+  if (mb <= 0) {
+    CANDMC_CK(cudaMemset2DAsync(T, sizeof(double) * ldt, 0, sizeof(double) * b1, b2, s));
+    return CANDMC_OK;
+  }
+  return gemm_tn_reduce(mref(Y1, ldy1), mref(Y2, ldy2), mb, (int)b1, b2, mref(nullptr, 0), 1.0, T,
+                        ldt, s);
+}
+
+int candmc_upd_A(const double* Y, int64_t ldy, double* A, int64_t lda, int64_t mb, int64_t kb,
+                 int64_t b, const double* W, int W_is_T, int precision, void* stream) {
+  if (!Y || !A || b < 1 || mb < 0 || kb < 0 || (mb > 0 && (ldy < mb || lda < mb)))
+    return set_error(CANDMC_ERR_ARG, "upd_A args");
+  return upd_core(Y, ldy, kDense, A, lda, mb, kb, b, W, W_is_T, precision, STREAM(stream));
+}
+
+int candmc_update_A(const double* Y, int64_t ldy, double* A, int64_t lda, int64_t m, int64_t k,
+                    int64_t b, const double* W, double* aggreg_Y, int64_t lda_aY, int W_is_T,
+                    int precision, void* stream) {
+  if (!Y || !A || b < 1 || m < 0 || k < 0 || (m > 0 && (ldy < m || lda < m)))
+    return set_error(CANDMC_ERR_ARG, "update_A args");
+  cudaStream_t s = STREAM(stream);
+  CANDMC_RET(upd_core(Y, ldy, kUnitLower, A, lda, m, k, b, W, W_is_T, precision, s));
+  if (aggreg_Y && m > 0) CANDMC_RET(materialize(mref(Y, ldy, 0, kUnitLower), m, b, aggreg_Y, lda_aY, s));
+  return CANDMC_OK;
+}
+
+int candmc_QR_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, double* aggreg_Y,
+                 int64_t lda_aY, int precision, void* stream) {
+  if (!A || b < 1 || k < 1 || m < k || lda < m) return set_error(CANDMC_ERR_ARG, "QR_2D args");
+  cudaStream_t s = STREAM(stream);
+  Status st;
+  CANDMC_RET(st.init(s));
+  return qr_2d_dev(A, lda, m, k, b, aggreg_Y, lda_aY, st.p(), precision, s);
+}
+
+int candmc_QR_2D_host(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int precision) {
+  if (!A || b < 1 || k < 1 || m < k || lda < m) return set_error(CANDMC_ERR_ARG, "QR_2D args");
+  CANDMC_RET(device_ok());
+  cudaStream_t s = nullptr;
+  int rc;
+  {
+    HostMat dA;
+    Status st;
+    CANDMC_RET(st.init(s));
+    CANDMC_RET(dA.in(A, lda, m, k, s));
+    CANDMC_RET(qr_2d_dev(dA.d.d(), dA.ldd, m, k, b, nullptr, 0, st.p(), precision, s));
+    CANDMC_RET(dA.out(A, lda, m, k, s));
+    rc = st.check(s);
+  }
+  CANDMC_CK(cudaStreamSynchronize(s));
+  return rc;
+}
+
+int candmc_QR_2D_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int64_t b_sub,
+                    double* aggreg_Y, int64_t lda_aY, int precision, void* stream) {
+  if (!A || b < 1 || b_sub < 1 || b % b_sub != 0 || k < 1 || m < k || lda < m)
+    return set_error(CANDMC_ERR_ARG, "QR_2D_2D args");
+  cudaStream_t s = STREAM(stream);
+  Status st;
+  CANDMC_RET(st.init(s));
+  // qr_2d.cxx:793-896: factor a b-wide block with QR_2D(b_sub), then update the
+  // rest once with the aggregated Y and T from Y^T Y (upd_A with W = NULL).
+  int64_t r0 = 0;
+  for (;;) {
+    const int64_t mm = m - r0, kk = k - r0;
+    double* P = A + r0 * lda + r0;
+    if (kk - b > 0 && mm - b > 0) {
+      CANDMC_RET(qr_2d_dev(P, lda, mm, b, b_sub, nullptr, 0, st.p(), precision, s));
+      if (aggreg_Y)
+        CANDMC_RET(materialize(mref(P, lda, 0, kUnitLower), mm, b, aggreg_Y + r0 * lda_aY + r0,
+                               lda_aY, s));
+      CANDMC_RET(upd_core(P, lda, kUnitLower, P + b * lda, lda, mm, kk - b, b, nullptr, 0,
+                          precision, s));
+      r0 += b;
+    } else {
+      CANDMC_RET(qr_2d_dev(P, lda, mm, kk, b_sub, aggreg_Y ? aggreg_Y + r0 * lda_aY + r0 : nullptr,
+                           lda_aY, st.p(), precision, s));
+      break;
+    }
+  }
+  return CANDMC_OK;
+}
+
+int candmc_QR_2D_pipe(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int precision,
+                      void* stream) {
+  return candmc_QR_2D(A, lda, m, k, b, nullptr, 0, precision, stream);
+}
+
+}  // extern "C"

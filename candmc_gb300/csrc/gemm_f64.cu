@@ -1,0 +1,299 @@
+// FP64 contractions of the CAQR trailing update and the small b x b products.
+//
+// Reference: upd_A (alg/QR/qr_2d/qr_2d.cxx:224-282) computes Z = Y^T*A with
+// dgemm (:259), all-reduces Z over the process column (:265), applies T^T by
+// dtrsm with T^-T (:271) and finishes with A -= Y*Z by dgemm (:275).  On one
+// GPU the all-reduce becomes a deterministic split-K reduction: each CTA of
+// gemm_tn owns a slice of rows and writes a partial Z, and reduce_apply sums
+// the partials in a fixed order and multiplies by T^T in the same pass.
+//
+// GB300 note: FP64 runs at ~1.2 TFLOP/s chip-wide (about 2 DFMA/clk/SM), so
+// these kernels are bound by the FP64 pipe, not by HBM (a 64x64 tile with
+// 4x4 register blocking needs only 8 shared loads per 16 DFMA).
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace candmc {
+
+constexpr int TM = 64, TN = 64, TK = 16;
+
+// out(i, j) = sum_{k in [k0, k1)} opA(i, k) * opB(k, j), 64 x 64 tile per CTA.
+// mode 0: store into out + split * split_stride (partials), ld ldo.
+// mode 1: out(i, j) -= result (out is the trailing matrix itself).
+__global__ void __launch_bounds__(kThreads)
+k_gemm_f64(MatRef A, MatRef B, int64_t M, int64_t N, int64_t K, int64_t kchunk, double* out,
+           int64_t ldo, int64_t split_stride, int mode) {
+  __shared__ double sA[TK][TM + 1];
+  __shared__ double sB[TK][TN + 1];
+  const int tid = threadIdx.x;
+  const int ti = tid % 16, tj = tid / 16;
+  const int64_t i0 = (int64_t)blockIdx.x * TM, j0 = (int64_t)blockIdx.y * TN;
+  const int64_t k0 = (int64_t)blockIdx.z * kchunk;
+  const int64_t k1 = (k0 + kchunk < K) ? k0 + kchunk : K;
+  double acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.0;
+
+  for (int64_t kb = k0; kb < k1; kb += TK) {
+    // A tile: TM x TK.  Coalesce along the stored row index.
+    for (int idx = tid; idx < TM * TK; idx += kThreads) {
+      int ii, kk;
+      if (A.trans) { kk = idx % TK; ii = idx / TK; } else { ii = idx % TM; kk = idx / TM; }
+      int64_t gi = i0 + ii, gk = kb + kk;
+      sA[kk][ii] = (gi < M && gk < k1) ? mat_at(A, gi, gk) : 0.0;
+    }
+    for (int idx = tid; idx < TK * TN; idx += kThreads) {
+      int jj, kk;
+      if (B.trans) { jj = idx % TN; kk = idx / TN; } else { kk = idx % TK; jj = idx / TK; }
+      int64_t gj = j0 + jj, gk = kb + kk;
+      sB[kk][jj] = (gj < N && gk < k1) ? mat_at(B, gk, gj) : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; ++kk) {
+      double a[4], bb[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = sA[kk][ti + 16 * u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) bb[v] = sB[kk][tj + 16 * v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], bb[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  double* o = out + (mode == 0 ? (int64_t)blockIdx.z * split_stride : 0);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    int64_t gi = i0 + ti + 16 * u;
+    if (gi >= M) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      int64_t gj = j0 + tj + 16 * v;
+      if (gj >= N) continue;
+      if (mode == 0) o[gj * ldo + gi] = acc[u][v];
+      else o[gj * ldo + gi] -= acc[u][v];
+    }
+  }
+}
+
+// Small-matrix product, 16 x 16 outputs per CTA, one per thread:
+// C(i,j) = alpha * sum_k opA(i,k) opB(k,j) + beta * C(i,j)   (beta == 0: C not read).
+__global__ void __launch_bounds__(kThreads)
+k_small_gemm(MatRef A, MatRef B, int64_t M, int64_t N, int64_t K, double alpha, double beta,
+             double* C, int64_t ldc) {
+  __shared__ double sA[16][65];
+  __shared__ double sB[64][17];
+  const int ti = threadIdx.x % 16, tj = threadIdx.x / 16;
+  const int64_t i0 = (int64_t)blockIdx.x * 16, j0 = (int64_t)blockIdx.y * 16;
+  double acc = 0.0;
+  for (int64_t kb = 0; kb < K; kb += 64) {
+    for (int idx = threadIdx.x; idx < 16 * 64; idx += kThreads) {
+      int ii = idx % 16, kk = idx / 16;
+      int64_t gi = i0 + ii, gk = kb + kk;
+      sA[ii][kk] = (gi < M && gk < K) ? mat_at(A, gi, gk) : 0.0;
+      int jj = idx / 64, k2 = idx % 64;
+      int64_t gj = j0 + jj, gk2 = kb + k2;
+      sB[k2][jj] = (gj < N && gk2 < K) ? mat_at(B, gk2, gj) : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 16
+    for (int kk = 0; kk < 64; ++kk) acc = fma(sA[ti][kk], sB[kk][tj], acc);
+    __syncthreads();
+  }
+  int64_t gi = i0 + ti, gj = j0 + tj;
+  if (gi < M && gj < N) {
+    double v = alpha * acc;
+    if (beta != 0.0) v += beta * C[gj * ldc + gi];
+    C[gj * ldc + gi] = v;
+  }
+}
+
+// Z(i,j) = alpha * sum_k opT(i,k) * (sum_s Zp[s](k,j))   with Zp[s] nb x n (ld nb);
+// opT == nullptr: identity.  16 x 16 outputs per CTA.
+__global__ void __launch_bounds__(kThreads)
+k_reduce_apply(const double* Zp, int nsplit, int64_t split_stride, int nb, int64_t n, MatRef Top,
+               double alpha, double* Z, int64_t ldz) {
+  extern __shared__ double sh[];
+  double* sZ = sh;               // nb x 16 (ld nb)
+  const int ti = threadIdx.x % 16, tj = threadIdx.x / 16;
+  const int64_t i0 = (int64_t)blockIdx.x * 16, j0 = (int64_t)blockIdx.y * 16;
+  for (int idx = threadIdx.x; idx < nb * 16; idx += kThreads) {
+    int k = idx % nb, jj = idx / nb;
+    int64_t gj = j0 + jj;
+    double s = 0.0;
+    if (gj < n)
+      for (int sp = 0; sp < nsplit; ++sp) s += Zp[sp * split_stride + gj * nb + k];
+    sZ[jj * nb + k] = s;
+  }
+  __syncthreads();
+  int64_t gi = i0 + ti, gj = j0 + tj;
+  if (gi >= nb || gj >= n) return;
+  double acc;
+  if (Top.p == nullptr) {
+    acc = sZ[tj * nb + gi];
+  } else {
+    acc = 0.0;
+    for (int k = 0; k < nb; ++k) acc = fma(mat_at(Top, gi, k), sZ[tj * nb + k], acc);
+  }
+  Z[gj * ldz + gi] = alpha * acc;
+}
+
+// Triangular inverse of an n x n matrix (ld), one column per thread.
+// lower != 0: lower triangular; unit != 0: unit diagonal implied.
+__global__ void k_tri_inv(const double* X, int64_t ldx, int n, int lower, int unit, double* Xi,
+                          int64_t ldi) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double* col = Xi + (int64_t)j * ldi;
+  if (lower) {
+    for (int i = 0; i < n; ++i) {
+      double acc;
+      if (i < j) {
+        acc = 0.0;
+      } else {
+        acc = (i == j) ? 1.0 : 0.0;
+        for (int k = j; k < i; ++k) acc -= X[(int64_t)k * ldx + i] * col[k];
+        if (!unit) acc /= X[(int64_t)i * ldx + i];
+      }
+      col[i] = acc;
+    }
+  } else {
+    for (int i = n - 1; i >= 0; --i) {
+      double acc;
+      if (i > j) {
+        acc = 0.0;
+      } else {
+        acc = (i == j) ? 1.0 : 0.0;
+        for (int k = i + 1; k <= j; ++k) acc -= X[(int64_t)k * ldx + i] * col[k];
+        if (!unit) acc /= X[(int64_t)i * ldx + i];
+      }
+      col[i] = acc;
+    }
+  }
+}
+
+// Copy op(X) (masked) into a dense n x k buffer (ld ldo).
+__global__ void k_materialize(MatRef X, int64_t n, int64_t k, double* out, int64_t ldo) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * k) return;
+  int64_t i = idx % n, j = idx / n;
+  out[j * ldo + i] = mat_at(X, i, j);
+}
+
+// T^-T from a Gram matrix: lower part of G with halved diagonal (qr_2d.cxx:46-51);
+// only the lower triangle (incl. diagonal) of T is written, as unpack_lower does.
+__global__ void k_invT_from_gram(const double* G, int64_t ldg, int b, double* T, int64_t ldt) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= b * b) return;
+  int i = idx % b, j = idx / b;
+  if (i < j) return;
+  double g = G[(int64_t)j * ldg + i];
+  T[(int64_t)j * ldt + i] = (i == j) ? 0.5 * g : g;
+}
+
+// out (n x k, ld) = identity (ones on the leading diagonal, zeros elsewhere)
+__global__ void k_set_identity(double* out, int64_t ld, int64_t n, int64_t k) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * k) return;
+  int64_t i = idx % n, j = idx / n;
+  out[j * ld + i] = (i == j) ? 1.0 : 0.0;
+}
+
+// ---------------------------------------------------------------- host side
+
+static int num_sms() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 148;
+  }
+  return n;
+}
+
+int small_gemm(int64_t M, int64_t N, int64_t K, double alpha, MatRef A, MatRef B, double beta,
+               double* C, int64_t ldc, cudaStream_t s) {
+  if (M <= 0 || N <= 0) return CANDMC_OK;
+  dim3 grid((unsigned)((M + 15) / 16), (unsigned)((N + 15) / 16));
+  k_small_gemm<<<grid, kThreads, 0, s>>>(A, B, M, N, K, alpha, beta, C, ldc);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+// Z (nb x n, ldz) = alpha * opT * (opY^T * opC), Y and C with m rows.
+// opT.p == nullptr means no triangular factor.
+int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top, double alpha,
+                   double* Z, int64_t ldz, cudaStream_t s) {
+  if (nb <= 0 || n <= 0) return CANDMC_OK;
+  if (nb > 256) return CANDMC_ERR_ARG;
+  const int64_t tiles = ((nb + TM - 1) / TM) * ((n + TN - 1) / TN);
+  const int64_t target = 2 * (int64_t)num_sms();
+  int64_t nsplit = std::max<int64_t>(1, std::min<int64_t>((target + tiles - 1) / tiles, (m + 255) / 256));
+  nsplit = std::min<int64_t>(nsplit, 1024);
+  int64_t kchunk = (m + nsplit - 1) / nsplit;
+  kchunk = ((kchunk + TK - 1) / TK) * TK;
+  nsplit = std::max<int64_t>(1, (m + kchunk - 1) / kchunk);
+  const int64_t stride = (int64_t)nb * n;
+  DevBuf part;
+  CANDMC_RET(part.alloc(sizeof(double) * (size_t)stride * nsplit, s));
+  MatRef Yt = Y;
+  Yt.trans = !Y.trans;   // element (i, r) of Y^T is Y(r, i)
+  dim3 grid((unsigned)((nb + TM - 1) / TM), (unsigned)((n + TN - 1) / TN), (unsigned)nsplit);
+  k_gemm_f64<<<grid, kThreads, 0, s>>>(Yt, C, nb, n, m, kchunk, part.d(), nb, stride, 0);
+  CANDMC_CK(cudaGetLastError());
+  dim3 g2((unsigned)((nb + 15) / 16), (unsigned)((n + 15) / 16));
+  size_t sm = sizeof(double) * (size_t)nb * 16;
+  k_reduce_apply<<<g2, kThreads, sm, s>>>(part.d(), (int)nsplit, stride, nb, n, Top, alpha, Z, ldz);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+// C (m x n, ldc) -= opY (m x nb) * Z (nb x n, ldz)
+int gemm_nn_sub(double* C, int64_t ldc, MatRef Y, const double* Z, int64_t ldz, int64_t m, int64_t n,
+                int nb, cudaStream_t s) {
+  if (m <= 0 || n <= 0 || nb <= 0) return CANDMC_OK;
+  dim3 grid((unsigned)((m + TM - 1) / TM), (unsigned)((n + TN - 1) / TN), 1);
+  k_gemm_f64<<<grid, kThreads, 0, s>>>(Y, mref(Z, ldz), m, n, nb, nb, C, ldc, 0, 1);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+int tri_inv(const double* X, int64_t ldx, int n, int lower, int unit, double* Xi, int64_t ldi,
+            cudaStream_t s) {
+  if (n <= 0) return CANDMC_OK;
+  k_tri_inv<<<(n + 127) / 128, 128, 0, s>>>(X, ldx, n, lower, unit, Xi, ldi);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+int materialize(MatRef X, int64_t n, int64_t k, double* out, int64_t ldo, cudaStream_t s) {
+  if (n <= 0 || k <= 0) return CANDMC_OK;
+  int64_t tot = n * k;
+  k_materialize<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, n, k, out, ldo);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+int set_identity(double* out, int64_t ld, int64_t n, int64_t k, cudaStream_t s) {
+  if (n <= 0 || k <= 0) return CANDMC_OK;
+  int64_t tot = n * k;
+  k_set_identity<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(out, ld, n, k);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+int invT_from_gram(const double* G, int64_t ldg, int b, double* T, int64_t ldt, cudaStream_t s) {
+  if (b <= 0) return CANDMC_OK;
+  k_invT_from_gram<<<(b * b + 255) / 256, 256, 0, s>>>(G, ldg, b, T, ldt);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+}  // namespace candmc

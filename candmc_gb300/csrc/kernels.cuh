@@ -1,0 +1,35 @@
+// Host-side launchers shared between the translation units of the library.
+#pragma once
+#include "common.cuh"
+
+namespace candmc {
+
+// panel.cu: direct TSQR-HR of an m x b panel, b <= kDirectB.
+int hr_direct(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
+              int64_t ldW, int* d_status, cudaStream_t s);
+
+// gemm_f64.cu
+int small_gemm(int64_t M, int64_t N, int64_t K, double alpha, MatRef A, MatRef B, double beta,
+               double* C, int64_t ldc, cudaStream_t s);
+int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top, double alpha,
+                   double* Z, int64_t ldz, cudaStream_t s);
+int gemm_nn_sub(double* C, int64_t ldc, MatRef Y, const double* Z, int64_t ldz, int64_t m,
+                int64_t n, int nb, cudaStream_t s);
+int tri_inv(const double* X, int64_t ldx, int n, int lower, int unit, double* Xi, int64_t ldi,
+            cudaStream_t s);
+int materialize(MatRef X, int64_t n, int64_t k, double* out, int64_t ldo, cudaStream_t s);
+int set_identity(double* out, int64_t ld, int64_t n, int64_t k, cudaStream_t s);
+int invT_from_gram(const double* G, int64_t ldg, int b, double* T, int64_t ldt, cudaStream_t s);
+
+// small.cu: signed LU and the dlarft recurrence.
+int signed_nlu(double* A, double* R, int64_t b, int64_t lda, int64_t ldr, int64_t* signs,
+               cudaStream_t s);
+int larft_from_gram(const double* G, int64_t ldg, const double* tau, int b, double* T,
+                    int64_t ldt, cudaStream_t s);
+
+// trailing update C <- (I - Y T Y^T)^T C in the requested arithmetic
+// (Y: unit-lower-trapezoidal m x nb read from a Y\R buffer; T upper nb x nb).
+int apply_qt(const double* Y, int64_t ldy, int64_t m, int nb, const double* T, int64_t ldT,
+             double* C, int64_t ldc, int64_t n, int precision, cudaStream_t s);
+
+}  // namespace candmc

@@ -1,0 +1,141 @@
+/*
+ * candmc_gb300.h -- C ABI of the GB300 (sm_103a) implementation of CANDMC's
+ * QR hot path: binary-tree TSQR, Householder reconstruction (TSQR-HR) and the
+ * CAQR trailing update A -= Y*T^T*(Y^T*A).
+ *
+ * Every function returns a status code (CANDMC_OK on success) and never
+ * throws.  Matrices are column-major float64 with a leading dimension, as in
+ * the reference.  Functions without a suffix take DEVICE pointers and run on
+ * the given CUDA stream (a cudaStream_t passed as void*, NULL = legacy default
+ * stream); they return once the work is enqueued.  Functions with the _host
+ * suffix take HOST pointers, copy in, compute and copy out, and return after
+ * the result is on the host.
+ *
+ * The reference's process grid (CommData_t / pview) collapses to one GPU: the
+ * entry points below are the reference functions at numPes == 1 (a 1 x 1
+ * grid), with the MPI arguments dropped.  The C++ drop-in with the reference's
+ * exact signatures (include/candmc/*.h) sits on top of these.
+ */
+#ifndef CANDMC_GB300_H
+#define CANDMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define CANDMC_OK 0
+#define CANDMC_ERR_ARG 1      /* invalid size, leading dimension or pointer */
+#define CANDMC_ERR_ALLOC 2    /* device or host allocation failed */
+#define CANDMC_ERR_CUDA 3     /* a CUDA runtime call or kernel launch failed */
+#define CANDMC_ERR_TIMEOUT 4  /* a bounded device-side wait ran out */
+#define CANDMC_ERR_NUMERIC 5  /* non-finite value or zero pivot detected */
+#define CANDMC_ERR_NODEV 6    /* no usable sm_103 device */
+
+/* arithmetic forms of the trailing-update contractions */
+#define CANDMC_PREC_FP64 0    /* plain FP64 (SIMT DFMA) */
+#define CANDMC_PREC_OZAKI 1   /* emulated FP64: BF16 Ozaki slices on tcgen05, FP32 accumulation */
+#define CANDMC_PREC_FP32 2    /* FP32 contraction (inputs rounded to FP32) */
+
+const char* candmc_status_string(int status);
+int candmc_version(void);
+/* last CUDA error text recorded by a failing call (thread-local) */
+const char* candmc_last_error(void);
+
+/* ---- TSQR-HR panel ------------------------------------------------------
+ * hh_recon_qr: alg/QR/hh_recon/hh_recon.h:66-75 (hh_recon.cxx:129-321).
+ * In: A (m x b, lda >= m, m >= b >= 1).  Out: A = Y\(S*R) -- Y strictly below
+ * the diagonal (unit diagonal implicit), S*R on and above it; W (b x b, ld b,
+ * upper) = U*S = -T*Y1^T.  T (b x b, ld b, upper, nullable) receives the
+ * compact-WY factor with Q = I - Y*T*Y^T.  Scratch is stream-ordered device
+ * memory released before return.
+ */
+int candmc_hh_recon_qr(double* A, int64_t lda, int64_t m, int64_t b, double* W, double* T,
+                       void* stream);
+int candmc_hh_recon_qr_host(double* A, int64_t lda, int64_t m, int64_t b, double* W, double* T);
+
+/* bitree_tsqr at numPes == 1: alg/QR/tsqr/bitree_tsqr.h:58-70 (bitree_tsqr.cxx:91-248).
+ * The single-rank tree is the leaf dgeqrf (bitree_tsqr.cxx:129-146): A becomes
+ * the LAPACK-form Householder QR Y\R (when output_Y), R (b x b, ld b, zero
+ * below the diagonal) and tau (b).  Computed by TSQR + reconstruction, so the
+ * reflectors are LAPACK's up to rounding (the last one of a square panel is
+ * the reconstruction's sign-choice reflector with tau = 2, as the reference's
+ * own tests note, test/QR/test_qr_2d.cxx:135-138). */
+int candmc_bitree_tsqr(double* A, int64_t lda, double* R, double* tau, int64_t m, int64_t b,
+                       int output_Y, void* stream);
+
+/* construct_Q1 at numPes == 1: alg/QR/tsqr/bitree_tsqr.h:91-104
+ * (construct_tsqr_Q.cxx:87-108, dorgqr): Q1 (m x k, ld ldq) = first k columns
+ * of Q = H_0...H_{b-1} from the reflectors in Y (lower part of a Y\R buffer)
+ * and tau.  k <= b. */
+int candmc_construct_Q1(const double* Y, int64_t ldy, const double* tau, double* Q1, int64_t ldq,
+                        int64_t m, int64_t b, int64_t k, void* stream);
+
+/* compute_invT_from_W: alg/QR/hh_recon/hh_recon.h:13-15 (hh_recon.cxx:26-31).
+ * invT (b x b, ld b) holds Y1 on entry and T^-T = -W^-T*Y1 on return. */
+int candmc_compute_invT_from_W(const double* W, int64_t b, double* invT, void* stream);
+
+/* signed_NLU / recursive_NLU: alg/QR/hh_recon/hh_recon.h:27-49
+ * (hh_recon.cxx:43-110).  Sign-choice unpivoted LU of (A - S), S_ii =
+ * -sign(A_ii); A (b x b, lda) becomes L\U, rows i of R (ldr) with S_ii = -1
+ * are negated, signs (int64, b, device) receives S_ii.  Both compute the same
+ * factorization (the recursion only reorders the arithmetic). */
+int candmc_signed_NLU(double* A, double* R, int64_t b, int64_t lda, int64_t ldr, int64_t* signs,
+                      void* stream);
+int candmc_recursive_NLU(double* A, double* R, int64_t b, int64_t lda, int64_t ldr,
+                         int64_t* signs, void* stream);
+
+/* ---- T factor ------------------------------------------------------------
+ * compute_invT_from_Y: alg/QR/qr_2d/qr_2d.h:25-31 (qr_2d.cxx:22-60).
+ * T (ldt) = stril(Y^T*Y) with the diagonal halved = T^-T, Y explicit mb x b. */
+int candmc_compute_invT_from_Y(const double* Y, int64_t ldy, double* T, int64_t ldt, int64_t mb,
+                               int64_t b, void* stream);
+/* rectangular form: alg/QR/qr_2d/qr_2d.h:47-56 (qr_2d.cxx:76-106): T = Y1^T*Y2 (b1 x b2). */
+int candmc_compute_invT_from_Y2(const double* Y1, int64_t ldy1, const double* Y2, int64_t ldy2,
+                                double* T, int64_t ldt, int64_t mb, int64_t b1, int64_t b2,
+                                void* stream);
+
+/* ---- CAQR trailing update -------------------------------------------------
+ * upd_A: alg/QR/qr_2d/qr_2d.h:99-108 (qr_2d.cxx:224-282).
+ * A (mb x kb, lda) <- (I - Y*T*Y^T)^T * A with Y explicit (mb x b, ldy: unit
+ * diagonal and zeros above it stored, as update_A packs it).  W selects T as
+ * in the reference: NULL -> T^-T from Y^T*Y; W_is_T == 0 -> W = -T*Y1^T;
+ * W_is_T != 0 -> W holds T^-T (lower).  precision: CANDMC_PREC_*. */
+int candmc_upd_A(const double* Y, int64_t ldy, double* A, int64_t lda, int64_t mb, int64_t kb,
+                 int64_t b, const double* W, int W_is_T, int precision, void* stream);
+
+/* update_A: alg/QR/qr_2d/qr_2d.h:74-85 (qr_2d.cxx:124-177).  Y is read from
+ * a Y\R buffer (strict lower part; unit diagonal implied).  A is m x k.
+ * aggreg_Y (nullable, lda_aY) receives the explicit Y (m x b). */
+int candmc_update_A(const double* Y, int64_t ldy, double* A, int64_t lda, int64_t m, int64_t k,
+                    int64_t b, const double* W, double* aggreg_Y, int64_t lda_aY, int W_is_T,
+                    int precision, void* stream);
+
+/* ---- full CAQR --------------------------------------------------------------
+ * QR_2D: alg/QR/qr_2d/qr_2d.h:124-131 (qr_2d.cxx:299-363) on a 1 x 1 grid.
+ * A (m x k, lda) becomes Y\R of all panels.  aggreg_Y (nullable, lda_aY)
+ * receives the explicit Y of every panel.  precision: CANDMC_PREC_*. */
+int candmc_QR_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, double* aggreg_Y,
+                 int64_t lda_aY, int precision, void* stream);
+int candmc_QR_2D_host(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int precision);
+
+/* QR_2D_2D: alg/QR/qr_2d/qr_2d.h:176-188 (qr_2d.cxx:772-897): two-level
+ * blocking, b a multiple of b_sub; each b-wide block is factored by QR_2D with
+ * panel width b_sub and the rest of the matrix is updated once per block with
+ * the aggregated Y and T = (T^-T from Y^T*Y)^-T. */
+int candmc_QR_2D_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int64_t b_sub,
+                    double* aggreg_Y, int64_t lda_aY, int precision, void* stream);
+
+/* QR_2D_pipe: alg/QR/qr_2d/qr_2d.h:293-302 (qr_2d.cxx:378-635).  On one GPU
+ * the lookahead pipeline computes the same factorization as QR_2D; the
+ * lookahead is realised by stream ordering. */
+int candmc_QR_2D_pipe(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int precision,
+                      void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CANDMC_GB300_H */

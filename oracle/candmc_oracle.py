@@ -300,13 +300,21 @@ def QR_2D(A, b):
     return Ws
 
 
-def tau_recon_lower(Y, b):
-    """tau_i = 2/(1 + ||Y[i+1:, i]||^2), 0 when that is 2 (alg/shared/util.cxx:437-466, 'L')."""
+def tau_recon_lower(Y, b, lapack_zero=False):
+    """tau_i = 2/(1 + ||Y[i+1:, i]||^2) (alg/shared/util.cxx:437-466, 'L').
+
+    The reference maps tau = 2 (an empty reflector tail) to 0, LAPACK's
+    choice for that case (lapack_zero=True).  Reconstruction keeps tau = 2
+    there: its sign choice S makes the reflector a sign flip, which is how
+    the last column of a square panel gets R_bb's sign (the reference's
+    test_qr_2d.cxx:135-138 notes the resulting difference from LAPACK).  The
+    checks below use the reconstruction convention.
+    """
     tau = np.zeros(b)
     for i in range(b):
         nrm = np.linalg.norm(Y[i + 1:, i])
         t = 2.0 / (nrm * nrm + 1.0)
-        tau[i] = 0.0 if t == 2.0 else t
+        tau[i] = 0.0 if (lapack_zero and t == 2.0) else t
     return tau
 
 
