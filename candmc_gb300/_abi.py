@@ -34,8 +34,17 @@ SIGNATURES = {
     "candmc_QR_2D_host": [_vp, _i64, _i64, _i64, _i64, _int],
     "candmc_QR_2D_2D": [_vp, _i64, _i64, _i64, _i64, _i64, _vp, _i64, _int, _vp],
     "candmc_QR_2D_pipe": [_vp, _i64, _i64, _i64, _i64, _int, _vp],
+    "candmc_launch_count": [],
+    "candmc_profile_begin": [ctypes.c_uint],
+    "candmc_profile_end": [_int, _vp, _vp, _vp],
 }
-_RESTYPES = {"candmc_status_string": ctypes.c_char_p, "candmc_last_error": ctypes.c_char_p}
+_RESTYPES = {"candmc_status_string": ctypes.c_char_p, "candmc_last_error": ctypes.c_char_p,
+             "candmc_launch_count": ctypes.c_longlong}
+
+# kernel classes of candmc_profile_begin / candmc_profile_end (CANDMC_KCLASS_*)
+KCLASS = {"gemm_tn": 0, "gemm_nn": 1, "reduce": 2, "panel_leaf": 3, "panel_y": 4, "small": 5,
+          "oz_slice": 6, "oz_tn": 7, "oz_nn": 8, "f32": 9}
+NKCLASS = 16
 
 _lib = None
 

@@ -33,8 +33,24 @@ int cuda_status(cudaError_t e, const char* where) {
   return CANDMC_ERR_CUDA;
 }
 
+// Once per device: keep freed stream-ordered scratch in the device's default
+// pool instead of returning it to the driver at every synchronisation, so a
+// repeated factorization reuses its scratch without re-mapping memory.
+static void ensure_pool() {
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev] = true;
+}
+
 int DevBuf::alloc(size_t bytes, cudaStream_t stream) {
   s = stream;
+  ensure_pool();
   if (bytes == 0) bytes = 16;
   cudaError_t e = cudaMallocAsync(&p, bytes, stream);
   if (e != cudaSuccess) {

@@ -222,6 +222,7 @@ int small_gemm(int64_t M, int64_t N, int64_t K, double alpha, MatRef A, MatRef B
                double* C, int64_t ldc, cudaStream_t s) {
   if (M <= 0 || N <= 0) return CANDMC_OK;
   dim3 grid((unsigned)((M + 15) / 16), (unsigned)((N + 15) / 16));
+  ProfScope ps(CANDMC_KCLASS_SMALL, 2.0 * M * N * K, s);
   k_small_gemm<<<grid, kThreads, 0, s>>>(A, B, M, N, K, alpha, beta, C, ldc);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
@@ -246,11 +247,17 @@ int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top,
   MatRef Yt = Y;
   Yt.trans = !Y.trans;   // element (i, r) of Y^T is Y(r, i)
   dim3 grid((unsigned)((nb + TM - 1) / TM), (unsigned)((n + TN - 1) / TN), (unsigned)nsplit);
-  k_gemm_f64<<<grid, kThreads, 0, s>>>(Yt, C, nb, n, m, kchunk, part.d(), nb, stride, 0);
+  {
+    ProfScope ps(CANDMC_KCLASS_GEMM_TN, 2.0 * nb * n * m, s);
+    k_gemm_f64<<<grid, kThreads, 0, s>>>(Yt, C, nb, n, m, kchunk, part.d(), nb, stride, 0);
+  }
   CANDMC_CK(cudaGetLastError());
   dim3 g2((unsigned)((nb + 15) / 16), (unsigned)((n + 15) / 16));
   size_t sm = sizeof(double) * (size_t)nb * 16;
-  k_reduce_apply<<<g2, kThreads, sm, s>>>(part.d(), (int)nsplit, stride, nb, n, Top, alpha, Z, ldz);
+  {
+    ProfScope ps(CANDMC_KCLASS_REDUCE, 8.0 * stride * nsplit, s);
+    k_reduce_apply<<<g2, kThreads, sm, s>>>(part.d(), (int)nsplit, stride, nb, n, Top, alpha, Z, ldz);
+  }
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
 }
@@ -260,6 +267,7 @@ int gemm_nn_sub(double* C, int64_t ldc, MatRef Y, const double* Z, int64_t ldz, 
                 int nb, cudaStream_t s) {
   if (m <= 0 || n <= 0 || nb <= 0) return CANDMC_OK;
   dim3 grid((unsigned)((m + TM - 1) / TM), (unsigned)((n + TN - 1) / TN), 1);
+  ProfScope ps(CANDMC_KCLASS_GEMM_NN, 2.0 * m * n * nb, s);
   k_gemm_f64<<<grid, kThreads, 0, s>>>(Y, mref(Z, ldz), m, n, nb, nb, C, ldc, 0, 1);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
@@ -268,6 +276,7 @@ int gemm_nn_sub(double* C, int64_t ldc, MatRef Y, const double* Z, int64_t ldz, 
 int tri_inv(const double* X, int64_t ldx, int n, int lower, int unit, double* Xi, int64_t ldi,
             cudaStream_t s) {
   if (n <= 0) return CANDMC_OK;
+  ProfScope ps(CANDMC_KCLASS_SMALL, 0.0, s);
   k_tri_inv<<<(n + 127) / 128, 128, 0, s>>>(X, ldx, n, lower, unit, Xi, ldi);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
@@ -276,6 +285,7 @@ int tri_inv(const double* X, int64_t ldx, int n, int lower, int unit, double* Xi
 int materialize(MatRef X, int64_t n, int64_t k, double* out, int64_t ldo, cudaStream_t s) {
   if (n <= 0 || k <= 0) return CANDMC_OK;
   int64_t tot = n * k;
+  ProfScope ps(CANDMC_KCLASS_SMALL, 16.0 * tot, s);
   k_materialize<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, n, k, out, ldo);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
@@ -284,6 +294,7 @@ int materialize(MatRef X, int64_t n, int64_t k, double* out, int64_t ldo, cudaSt
 int set_identity(double* out, int64_t ld, int64_t n, int64_t k, cudaStream_t s) {
   if (n <= 0 || k <= 0) return CANDMC_OK;
   int64_t tot = n * k;
+  ProfScope ps(CANDMC_KCLASS_SMALL, 8.0 * tot, s);
   k_set_identity<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(out, ld, n, k);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
@@ -291,6 +302,7 @@ int set_identity(double* out, int64_t ld, int64_t n, int64_t k, cudaStream_t s) 
 
 int invT_from_gram(const double* G, int64_t ldg, int b, double* T, int64_t ldt, cudaStream_t s) {
   if (b <= 0) return CANDMC_OK;
+  ProfScope ps(CANDMC_KCLASS_SMALL, 0.0, s);
   k_invT_from_gram<<<(b * b + 255) / 256, 256, 0, s>>>(G, ldg, b, T, ldt);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;

@@ -4,6 +4,23 @@
 
 namespace candmc {
 
+// prof.cu: every launch goes through a ProfScope (launch count + optional
+// CUDA-event timing of its class on the launching stream).  Class ids are the
+// CANDMC_KCLASS_* values of the public header.
+constexpr int kProfClasses = 16;
+void count_launch();
+bool prof_on(int cls);
+class ProfScope {
+ public:
+  ProfScope(int cls, double work, cudaStream_t s);
+  ~ProfScope();
+ private:
+  int cls_;
+  double work_;
+  cudaStream_t s_;
+  cudaEvent_t e0_{}, e1_{};
+};
+
 // panel.cu: direct TSQR-HR of an m x b panel, b <= kDirectB.
 int hr_direct(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
               int64_t ldW, int* d_status, cudaStream_t s);

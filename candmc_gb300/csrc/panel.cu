@@ -24,7 +24,7 @@
 
 #include <algorithm>
 
-#include "common.cuh"
+#include "kernels.cuh"
 
 namespace candmc {
 
@@ -389,10 +389,17 @@ int hr_direct(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, 
   a.status = d_status; a.tree = tree;
   CANDMC_CK(cudaFuncSetAttribute(hr_leaf_tree, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sm_leaf));
-  hr_leaf_tree<<<(unsigned)P, kThreads, sm_leaf, s>>>(a);
+  {
+    // algorithmic work: leaf QR + explicit leaf Q (~4 m b^2) and the tree nodes
+    ProfScope ps(CANDMC_KCLASS_PANEL_LEAF, 4.0 * m * b * b, s);
+    hr_leaf_tree<<<(unsigned)P, kThreads, sm_leaf, s>>>(a);
+  }
   CANDMC_CK(cudaGetLastError());
   size_t sm_y = sizeof(double) * 3 * nb2;
-  hr_form_y<<<(unsigned)P, kThreads, sm_y, s>>>(a);
+  {
+    ProfScope ps(CANDMC_KCLASS_PANEL_Y, 1.0 * m * b * b, s);
+    hr_form_y<<<(unsigned)P, kThreads, sm_y, s>>>(a);
+  }
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
 }

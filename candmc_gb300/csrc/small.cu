@@ -62,6 +62,7 @@ int signed_nlu(double* A, double* R, int64_t b, int64_t lda, int64_t ldr, int64_
   } else {
     sm = 0;
   }
+  ProfScope ps(CANDMC_KCLASS_SMALL, 0.0, s);
   k_signed_nlu<<<1, kThreads, sm, s>>>(A, R, (int)b, lda, ldr, signs, use_smem,
                                         static_cast<int*>(st.p));
   CANDMC_CK(cudaGetLastError());
@@ -93,6 +94,7 @@ k_larft(const double* G, int64_t ldg, const double* tau, int b, double* T, int64
 int larft_from_gram(const double* G, int64_t ldg, const double* tau, int b, double* T,
                     int64_t ldt, cudaStream_t s) {
   if (b <= 0) return CANDMC_OK;
+  ProfScope ps(CANDMC_KCLASS_SMALL, 0.0, s);
   k_larft<<<1, kThreads, 0, s>>>(G, ldg, tau, b, T, ldt);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;

@@ -44,6 +44,29 @@ int candmc_version(void);
 /* last CUDA error text recorded by a failing call (thread-local) */
 const char* candmc_last_error(void);
 
+/* ---- launch accounting (no counterpart in the reference, which times phases
+ * with CTF timers, alg/shared/timer.h:21-35) ---------------------------------
+ * candmc_launch_count: kernels this library has launched since load.
+ * candmc_profile_begin(mask): from now on, bracket every launch of a kernel
+ * class whose bit is set in mask with CUDA events on its launching stream.
+ * candmc_profile_end: synchronises those events, writes per class (index <
+ * ncls) the summed kernel milliseconds, the summed algorithmic work (flops
+ * for contractions, bytes for memory-bound kernels) and the launch count, and
+ * stops recording. */
+#define CANDMC_KCLASS_GEMM_TN 0     /* FP64 split-K Z = Y^T A partials */
+#define CANDMC_KCLASS_GEMM_NN 1     /* FP64 A -= Y Z */
+#define CANDMC_KCLASS_REDUCE 2      /* split-K reduction + T^T */
+#define CANDMC_KCLASS_PANEL_LEAF 3  /* TSQR leaves + tree + reconstruction */
+#define CANDMC_KCLASS_PANEL_Y 4     /* Y = Q_leaf * (chain * U^-1) */
+#define CANDMC_KCLASS_SMALL 5       /* b x b products, inverses, copies */
+#define CANDMC_KCLASS_OZ_SLICE 6    /* Ozaki: FP64 -> BF16 slices */
+#define CANDMC_KCLASS_OZ_TN 7       /* Ozaki: Z = Y^T A on tcgen05 */
+#define CANDMC_KCLASS_OZ_NN 8       /* Ozaki: A -= Y Z on tcgen05 */
+#define CANDMC_KCLASS_F32 9         /* FP32-form contractions */
+long long candmc_launch_count(void);
+int candmc_profile_begin(unsigned mask);
+int candmc_profile_end(int ncls, double* ms, double* work, long long* launches);
+
 /* ---- TSQR-HR panel ------------------------------------------------------
  * hh_recon_qr: alg/QR/hh_recon/hh_recon.h:66-75 (hh_recon.cxx:129-321).
  * In: A (m x b, lda >= m, m >= b >= 1).  Out: A = Y\(S*R) -- Y strictly below

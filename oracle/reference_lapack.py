@@ -1,0 +1,154 @@
+"""The reference's single-rank CAQR call sequence, executed with LAPACK/BLAS.
+
+TEST INFRASTRUCTURE ONLY: the CPU baseline of bench.py (cpu_baseline and
+`--impl reference`).  CANDMC itself is not compiled here (its QR path needs
+MPI and a LAPACK, both external libraries), so this module replays, call for
+call and with the same leading dimensions, what its QR_2D does on a 1 x 1
+process grid.  The LAPACK/BLAS routines are the Fortran entry points of the
+OpenBLAS build bundled with scipy (LP64; `scipy_` symbol prefix), called
+through ctypes with pointers into the column-major matrix, as the reference's
+wrappers in alg/shared/lapack.cxx do.  OpenBLAS uses every host thread.
+
+  QR_2D (alg/QR/qr_2d/qr_2d.cxx:299-363), per panel:
+    hh_recon_qr (alg/QR/hh_recon/hh_recon.cxx:129-321):
+      bitree_tsqr with np_work == 1: copy the panel, dgeqrf   (bitree_tsqr.cxx:129-146)
+      construct_Q1 with np_work == 1: copy Y, dorgqr           (construct_tsqr_Q.cxx:87-96)
+      recursive_NLU on Q1's top block                          (hh_recon.cxx:282)
+      Y2 = Q2 U^-1 by dtrsm, Y and S*R back into A             (hh_recon.cxx:284-302)
+      W = U S                                                  (hh_recon.cxx:304-310)
+    update_A (qr_2d.cxx:124-177): pack Ybuf with a unit diagonal, then
+    upd_A (qr_2d.cxx:224-282): T^-T from W by dtrsm (comp_bcast_T_from_W,
+      :179-208), Z = Y^T A by dgemm (:259), Z <- (T^-T)^-1 Z by dtrsm (:271),
+      A -= Y Z by dgemm (:275).
+"""
+import ctypes
+import glob
+import os
+
+import numpy as np
+
+from . import candmc_oracle as co
+
+_lib = None
+_c_int = ctypes.c_int
+_c_dbl = ctypes.c_double
+_c_chr = ctypes.c_char
+
+
+def _openblas():
+    global _lib
+    if _lib is None:
+        import scipy
+        d = os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs")
+        cands = sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so")))
+        if not cands:
+            raise RuntimeError("scipy's bundled OpenBLAS was not found")
+        _lib = ctypes.CDLL(cands[0])
+    return _lib
+
+
+def blas_threads():
+    return int(_openblas().scipy_openblas_get_num_threads())
+
+
+def _p(a, off=0):
+    return ctypes.c_void_p(a.ctypes.data + 8 * off)
+
+
+def _ref(x, t):
+    return ctypes.byref(t(x))
+
+
+def dgemm(ta, tb, m, n, k, alpha, A, offA, lda, B, offB, ldb, beta, C, offC, ldc):
+    _openblas().scipy_dgemm_(_ref(ta.encode(), _c_chr), _ref(tb.encode(), _c_chr),
+                             _ref(m, _c_int), _ref(n, _c_int), _ref(k, _c_int), _ref(alpha, _c_dbl),
+                             _p(A, offA), _ref(lda, _c_int), _p(B, offB), _ref(ldb, _c_int),
+                             _ref(beta, _c_dbl), _p(C, offC), _ref(ldc, _c_int))
+
+
+def dtrsm(side, uplo, ta, diag, m, n, alpha, A, offA, lda, B, offB, ldb):
+    _openblas().scipy_dtrsm_(_ref(side.encode(), _c_chr), _ref(uplo.encode(), _c_chr),
+                             _ref(ta.encode(), _c_chr), _ref(diag.encode(), _c_chr),
+                             _ref(m, _c_int), _ref(n, _c_int), _ref(alpha, _c_dbl),
+                             _p(A, offA), _ref(lda, _c_int), _p(B, offB), _ref(ldb, _c_int))
+
+
+def dgeqrf(m, n, A, lda, tau):
+    lwork = max(1, 64 * n)
+    work = np.empty(lwork)
+    info = _c_int(0)
+    _openblas().scipy_dgeqrf_(_ref(m, _c_int), _ref(n, _c_int), _p(A), _ref(lda, _c_int), _p(tau),
+                              _p(work), _ref(lwork, _c_int), ctypes.byref(info))
+    assert info.value == 0
+
+
+def dorgqr(m, n, k, A, lda, tau):
+    lwork = max(1, 64 * n)
+    work = np.empty(lwork)
+    info = _c_int(0)
+    _openblas().scipy_dorgqr_(_ref(m, _c_int), _ref(n, _c_int), _ref(k, _c_int), _p(A),
+                              _ref(lda, _c_int), _p(tau), _p(work), _ref(lwork, _c_int),
+                              ctypes.byref(info))
+    assert info.value == 0
+
+
+def _flat(A):
+    """1-D view of a Fortran array's storage (for pointer arithmetic)."""
+    assert A.flags.f_contiguous
+    return A.reshape(-1, order="F")
+
+
+def hh_recon_qr_lapack(Af, lda, off, m, b):
+    """hh_recon_qr at numPes == 1 on the m x b panel at offset `off` of Af; returns W."""
+    buf = np.empty((m, b), order="F")
+    for j in range(b):
+        buf[:, j] = Af[off + j * lda: off + j * lda + m]
+    tau = np.empty(b)
+    dgeqrf(m, b, buf, m, tau)
+    R = np.triu(buf[:b, :b])
+    dorgqr(m, b, b, buf, m, tau)                     # buf now holds Q1 (lda = m)
+    top = np.array(buf[:b, :b], order="F")
+    signs = co.recursive_NLU(top, R)
+    U = np.array(np.triu(top), order="F")
+    if m > b:
+        dtrsm("R", "U", "N", "N", m - b, b, 1.0, U, 0, b, buf, b, m)
+    buf[:b, :b] = np.tril(top, -1) + np.triu(R)
+    for j in range(b):
+        col = buf[:, j].copy()
+        col[:j] = buf[:j, j]
+        Af[off + j * lda: off + j * lda + m] = col
+    return np.array(U * signs[None, :], order="F")
+
+
+def upd_A_lapack(Af, lda, offY, offA, m, k, b, W):
+    """update_A + upd_A with W from hh_recon_qr (qr_2d.cxx:124-177, 224-282)."""
+    Ybuf = np.zeros((m, b), order="F")
+    for j in range(b):
+        Ybuf[j + 1:, j] = Af[offY + j * lda + j + 1: offY + j * lda + m]
+        Ybuf[j, j] = 1.0
+    X = np.array(Ybuf[:b, :b], order="F")
+    dtrsm("L", "U", "T", "N", b, b, -1.0, W, 0, b, X, 0, b)        # W^T X = -Y1
+    X = np.array(np.tril(X), order="F")
+    Z = np.empty((b, k), order="F")
+    dgemm("T", "N", b, k, m, 1.0, Ybuf, 0, m, Af, offA, lda, 0.0, Z, 0, b)
+    dtrsm("L", "L", "N", "N", b, k, 1.0, X, 0, b, Z, 0, b)
+    dgemm("N", "N", m, k, b, -1.0, Ybuf, 0, m, Z, 0, b, 1.0, Af, offA, lda)
+
+
+def QR_2D_lapack(A, b):
+    """QR_2D on a 1 x 1 grid; A (Fortran float64, m x k, m >= k) becomes Y\\R in place."""
+    m, k = A.shape
+    lda = m
+    Af = _flat(A)
+    r0 = 0
+    while True:
+        mm, kk = m - r0, k - r0
+        bb = min(kk, b)
+        off = r0 * lda + r0
+        W = hh_recon_qr_lapack(Af, lda, off, mm, bb)
+        if kk - b > 0 and mm - b > 0:
+            upd_A_lapack(Af, lda, off, off + b * lda, mm, kk - b, b, W)
+            r0 += b
+        else:
+            break
+    return A
