@@ -404,4 +404,51 @@ int hr_direct(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, 
   return CANDMC_OK;
 }
 
+// Same two kernels as hr_direct, on scratch the caller provides (no
+// allocation here).  P leaves of at most 256 rows.  The caller zeroes cnt and
+// the status word before the launch and guarantees the scratch sizes of
+// hr_prealloc_sizes().
+void hr_prealloc_sizes(int64_t m, int b, int64_t* P, int64_t* nnodes) {
+  int64_t p = (m + 255) / 256;
+  if (p > m / b) p = m / b;
+  if (p < 1) p = 1;
+  *P = p;
+  *nnodes = make_tree((int)p).nnodes;
+}
+
+int hr_direct_prealloc(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
+                       int64_t ldW, double* Qw, double* Rn, double* Q11, double* Q21,
+                       unsigned* cnt, double* Uinv, int* d_status, cudaStream_t s) {
+  if (b < 1 || b > kDirectB || m < b) return CANDMC_ERR_ARG;
+  int64_t P, nn;
+  hr_prealloc_sizes(m, b, &P, &nn);
+  TreeDesc tree = make_tree((int)P);
+  const int64_t Lmax = (m + P - 1) / P;
+  size_t sm_leaf = sizeof(double) * (size_t)std::max<int64_t>(Lmax * b, 4 * (int64_t)b * b);
+  if (sm_leaf > 200 * 1024) return CANDMC_ERR_ARG;
+  HrArgs a;
+  a.A = A; a.lda = lda; a.m = m; a.b = b;
+  a.Qw = Qw; a.Rn = Rn; a.Q11 = Q11; a.Q21 = Q21; a.cnt = cnt;
+  a.T = T; a.ldT = ldT; a.W = W; a.ldW = ldW; a.Uinv = Uinv;
+  a.status = d_status; a.tree = tree;
+  {
+    ProfScope ps(CANDMC_KCLASS_PANEL_LEAF, 4.0 * m * b * b, s);
+    hr_leaf_tree<<<(unsigned)P, kThreads, sm_leaf, s>>>(a);
+  }
+  CANDMC_CK(cudaGetLastError());
+  {
+    ProfScope ps(CANDMC_KCLASS_PANEL_Y, 1.0 * m * b * b, s);
+    hr_form_y<<<(unsigned)P, kThreads, sizeof(double) * 3 * (size_t)b * b, s>>>(a);
+  }
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+// Raise the leaf kernel's dynamic shared-memory limit (no allocation).
+int hr_prealloc_setup() {
+  CANDMC_CK(cudaFuncSetAttribute(hr_leaf_tree, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024));
+  return CANDMC_OK;
+}
+
 }  // namespace candmc

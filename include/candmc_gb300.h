@@ -79,6 +79,20 @@ int candmc_hh_recon_qr(double* A, int64_t lda, int64_t m, int64_t b, double* W, 
                        void* stream);
 int candmc_hh_recon_qr_host(double* A, int64_t lda, int64_t m, int64_t b, double* W, double* T);
 
+/* candmc_hh_recon_qr_noalloc: no counterpart in the reference.  The same
+ * TSQR-HR as candmc_hh_recon_qr (same arguments; W and T required), for
+ * callers that cannot let a library allocate device memory during their run,
+ * e.g. a server that budgets all GPU memory at start-up or a framework whose
+ * own allocator must own every device buffer.  It allocates nothing: its
+ * scratch is a fixed array of about 3.7 MB inside the library, held on every
+ * GPU that loads the library until exit.  Limits: 1 <= b <= 32 and
+ * b <= m <= 8192; larger sizes return CANDMC_ERR_ARG.  All calls share that
+ * array, so calls that overlap on the GPU race: serialize them.  The first
+ * call on a device sets up that device (looks up the array's address); make
+ * it before any stream capture begins. */
+int candmc_hh_recon_qr_noalloc(double* A, int64_t lda, int64_t m, int64_t b, double* W, double* T,
+                               void* stream);
+
 /* bitree_tsqr at numPes == 1: alg/QR/tsqr/bitree_tsqr.h:58-70 (bitree_tsqr.cxx:91-248).
  * The single-rank tree is the leaf dgeqrf (bitree_tsqr.cxx:129-146): A becomes
  * the LAPACK-form Householder QR Y\R (when output_Y), R (b x b, ld b, zero
