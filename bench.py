@@ -63,7 +63,14 @@ def flops(n):
 # ----------------------------------------------------------------- inputs
 def make_input_gpu(n, seed, sigma_min, device):
     """A = U diag(sigma) V^T, U and V Haar from PCG64(seed) (U first), on the GPU."""
+    import ctypes
+
     import torch
+    # torch loads its CUDA linear-algebra library lazily by bare name; load it
+    # by path first so the lookup also succeeds under a profiler's injection.
+    linalg = os.path.join(os.path.dirname(torch.__file__), "lib", "libtorch_cuda_linalg.so")
+    if os.path.exists(linalg):
+        ctypes.CDLL(linalg, mode=ctypes.RTLD_GLOBAL)
     rng = np.random.default_rng(seed)
     mats = []
     for _ in range(2):
