@@ -64,6 +64,23 @@ DevBuf::~DevBuf() {
   if (p) cudaFreeAsync(p, s);
 }
 
+// Per-call device status word.
+struct Status {
+  DevBuf buf;
+  int init(cudaStream_t s) {
+    CANDMC_RET(buf.alloc(sizeof(int), s));
+    CANDMC_CK(cudaMemsetAsync(buf.p, 0, sizeof(int), s));
+    return CANDMC_OK;
+  }
+  int* p() { return static_cast<int*>(buf.p); }
+  int check(cudaStream_t s) {
+    int h = 0;
+    CANDMC_CK(cudaMemcpyAsync(&h, buf.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CANDMC_CK(cudaStreamSynchronize(s));
+    return h;
+  }
+};
+
 // C <- (I - Y T Y^T)^T C = C - Y * (T^T * (Y^T * C))
 int apply_qt(const double* Y, int64_t ldy, int64_t m, int nb, const double* T, int64_t ldT,
              double* C, int64_t ldc, int64_t n, int precision, cudaStream_t s);
@@ -75,7 +92,8 @@ static int hr_rec(double* A, int64_t lda, int64_t m, int b, double* T, int64_t l
   if (b <= kDirectB) return hr_direct(A, lda, m, b, T, ldT, nullptr, 0, st, s);
   const int b1 = b / 2, b2 = b - b1;
   CANDMC_RET(hr_rec(A, lda, m, b1, T, ldT, st, precision, s));
-  CANDMC_RET(apply_qt(A, lda, m, b1, T, ldT, A + (int64_t)b1 * lda, lda, b2, precision, s));
+  // the panel itself stays in FP64 (its updates are m x b/2 x b/2: small)
+  CANDMC_RET(apply_qt(A, lda, m, b1, T, ldT, A + (int64_t)b1 * lda, lda, b2, CANDMC_PREC_FP64, s));
   double* T22 = T + (int64_t)b1 * ldT + b1;
   CANDMC_RET(hr_rec(A + (int64_t)b1 * lda + b1, lda, m - b1, b2, T22, ldT, st, precision, s));
   // G = Y1[b1:m, :]^T * Y2   (Y2 unit-lower in A[b1:, b1:])
@@ -151,11 +169,21 @@ static int upd_core(const double* Y, int64_t ldy, int ymask, double* A, int64_t 
                     int64_t kb, int64_t b, const double* W, int W_is_T, int precision,
                     cudaStream_t s) {
   if (mb <= 0 || kb <= 0) return CANDMC_OK;
-  if (precision != CANDMC_PREC_FP64) return set_error(CANDMC_ERR_ARG, "precision form not built");
+  if (precision != CANDMC_PREC_FP64 && precision != CANDMC_PREC_OZAKI)
+    return set_error(CANDMC_ERR_ARG, "precision form not built");
   DevBuf top, z;
   CANDMC_RET(top.alloc(sizeof(double) * b * b, s));
-  CANDMC_RET(z.alloc(sizeof(double) * b * kb, s));
   CANDMC_RET(top_from_W(Y, ldy, mb, b, W, W_is_T, ymask, top.d(), s));
+  if (precision == CANDMC_PREC_OZAKI) {
+    if (b > 128) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
+    Status st;
+    CANDMC_RET(st.init(s));
+    CANDMC_RET(to_df64(A, lda, mb, kb, s));
+    CANDMC_RET(apply_qt_ozaki(Y, ldy, ymask, mb, (int)b, mref(top.d(), b, 0, kLower), A, lda, kb, 0,
+                              st.p(), s));
+    return from_df64(A, lda, mb, kb, s);
+  }
+  CANDMC_RET(z.alloc(sizeof(double) * b * kb, s));
   MatRef Ym = mref(Y, ldy, 0, ymask);
   CANDMC_RET(gemm_tn_reduce(Ym, mref(A, lda), mb, (int)b, kb, mref(top.d(), b, 0, kLower), 1.0,
                             z.d(), b, s));
@@ -167,17 +195,29 @@ static int qr_2d_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, do
                      int64_t lda_aY, int* st, int precision, cudaStream_t s) {
   DevBuf tb;
   CANDMC_RET(tb.alloc(sizeof(double) * b * b, s));
+  const bool oz = (precision == CANDMC_PREC_OZAKI);
+  if (precision != CANDMC_PREC_FP64 && !oz) return set_error(CANDMC_ERR_ARG, "precision form not built");
+  if (oz && b > 128) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
+  // emulated form: the not-yet-factored part lives as df64 pairs; each panel is
+  // turned back into FP64 before its reconstruction, and the trailing update
+  // writes the finished R rows as FP64.
+  if (oz) CANDMC_RET(to_df64(A, lda, m, k, s));
   int64_t r0 = 0;
   for (;;) {
     const int64_t mm = m - r0, kk = k - r0;
     const int64_t bb = std::min(kk, b);
     double* P = A + r0 * lda + r0;
+    if (oz) CANDMC_RET(from_df64(P, lda, mm, bb, s));
     CANDMC_RET(hr_rec(P, lda, mm, (int)bb, tb.d(), b, st, precision, s));
     if (aggreg_Y)
       CANDMC_RET(materialize(mref(P, lda, 0, kUnitLower), mm, bb, aggreg_Y + r0 * lda_aY + r0,
                              lda_aY, s));
     if (kk - b > 0 && mm - b > 0) {
-      CANDMC_RET(apply_qt(P, lda, mm, (int)b, tb.d(), b, P + b * lda, lda, kk - b, precision, s));
+      if (oz)
+        CANDMC_RET(apply_qt_ozaki(P, lda, kUnitLower, mm, (int)b, mref(tb.d(), b, 1, kUpper),
+                                  P + b * lda, lda, kk - b, b, st, s));
+      else
+        CANDMC_RET(apply_qt(P, lda, mm, (int)b, tb.d(), b, P + b * lda, lda, kk - b, precision, s));
       r0 += b;
     } else {
       break;
@@ -185,23 +225,6 @@ static int qr_2d_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, do
   }
   return CANDMC_OK;
 }
-
-// Per-call device status word.
-struct Status {
-  DevBuf buf;
-  int init(cudaStream_t s) {
-    CANDMC_RET(buf.alloc(sizeof(int), s));
-    CANDMC_CK(cudaMemsetAsync(buf.p, 0, sizeof(int), s));
-    return CANDMC_OK;
-  }
-  int* p() { return static_cast<int*>(buf.p); }
-  int check(cudaStream_t s) {
-    int h = 0;
-    CANDMC_CK(cudaMemcpyAsync(&h, buf.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CANDMC_CK(cudaStreamSynchronize(s));
-    return h;
-  }
-};
 
 static int device_ok() {
   int n = 0;

@@ -44,6 +44,15 @@ int signed_nlu(double* A, double* R, int64_t b, int64_t lda, int64_t ldr, int64_
 int larft_from_gram(const double* G, int64_t ldg, const double* tau, int b, double* T,
                     int64_t ldt, cudaStream_t s);
 
+// ozaki.cu: emulated-FP64 trailing update on tcgen05.  C holds df64 pairs
+// (float hi, float lo in each 8-byte slot); rows < fp64_rows are written back
+// as FP64.  Top is the operator T^T applied to Y^T C.
+int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
+                   double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
+                   cudaStream_t s);
+int to_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
+int from_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
+
 // trailing update C <- (I - Y T Y^T)^T C in the requested arithmetic
 // (Y: unit-lower-trapezoidal m x nb read from a Y\R buffer; T upper nb x nb).
 int apply_qt(const double* Y, int64_t ldy, int64_t m, int nb, const double* T, int64_t ldT,

@@ -1,0 +1,630 @@
+// Emulated-FP64 contractions of the CAQR trailing update on the 5th-generation
+// tensor cores (tcgen05, BF16 inputs, FP32 accumulation in TMEM).
+//
+// Ozaki-style splitting (Ozaki, Ogita, Oishi, Rump, "Error-free transformations
+// of matrix multiplication by using fast routines of matrix multiplication and
+// its applications", Numer. Algorithms 59, 2012): every operand element x of a
+// scale group with |x| < 2^e is written as x = 2^(e-8) * sum_{i<7} d_i 2^(-8i)
+// with balanced integer digits |d_0| <= 256, |d_i| <= 128 (i >= 1).  Slice i
+// holds d_i * 2^(-8i), exact in BF16 (<= 8 significant bits).  A product of
+// two slices has <= 16 significant bits, so a K = 128 sum of one "level"
+// L = i + j is an exact FP32 integer (at its weight); levels 0..3 get one TMEM
+// accumulator each and levels 4..6 share a fifth (their rounding sits below
+// 2^-56 of the result).  28 slice pairs (i + j <= 6) are issued per K step.
+//
+// The trailing matrix is held as float pairs (hi, lo) ("df64", ~48 bits)
+// during the emulated factorization, so no epilogue needs the GB300's slow
+// FP64 pipe: groups are combined, scaled and subtracted with FP32 TwoSum
+// arithmetic.  Finished rows (the panel's R block) are written back as FP64.
+//
+// Kernel layout (k_oz_mma): one CTA per 128 x 96 output tile and K split,
+// 256 threads.  Operand slices are pre-sliced in global memory in the UMMA
+// "K-major, no swizzle" core-matrix order, so each K16 step of a tile is a
+// contiguous 4 KB (A, 128 rows) and 3 KB (B, 96 rows) block per slice;
+// threads copy them with cp.async into a 3-stage shared-memory ring, one
+// elected thread issues the 28 tcgen05.mma of a step and commits them to the
+// stage's mbarrier.  Every wait is bounded; a wait that runs out sets the
+// status word, the CTA drains and frees its TMEM and returns.
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include <algorithm>
+
+#include "kernels.cuh"
+
+namespace candmc {
+
+constexpr int OZ_S = 7;           // slices per operand
+constexpr int OZ_G = 5;           // TMEM accumulator groups
+constexpr int OZ_M = 128;         // tile rows (TMEM lanes)
+constexpr int OZ_N = 96;          // tile columns
+constexpr int OZ_STAGES = 3;
+constexpr int OZ_ABYTES = OZ_M * 16 * 2;               // one slice, one K16 step
+constexpr int OZ_BBYTES = OZ_N * 16 * 2;
+constexpr int OZ_STAGE_BYTES = OZ_S * (OZ_ABYTES + OZ_BBYTES);
+constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024;
+constexpr long OZ_WAIT_LIMIT = 1L << 22;                // bounded mbarrier polls
+
+// element (r, k) of an R x K operand slice plane in core-matrix K-major order
+__host__ __device__ __forceinline__ int64_t cm_off(int64_t r, int64_t k, int64_t R) {
+  return (k >> 4) * (R * 16) + (r >> 3) * 128 + ((k & 15) >> 3) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// ------------------------------------------------------------------ df64
+struct f2 {
+  float h, l;
+};
+
+__device__ __forceinline__ f2 two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+
+__device__ __forceinline__ f2 fast_two_sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+
+// (h, l) + g
+__device__ __forceinline__ f2 df_add_f(f2 x, float g) {
+  f2 s = two_sum(x.h, g);
+  return fast_two_sum(s.h, s.l + x.l);
+}
+
+// x + y
+__device__ __forceinline__ f2 df_add(f2 x, f2 y) {
+  f2 s = two_sum(x.h, y.h);
+  f2 t = two_sum(x.l, y.l);
+  s.l += t.h;
+  s = fast_two_sum(s.h, s.l);
+  s.l += t.l;
+  return fast_two_sum(s.h, s.l);
+}
+
+__device__ __forceinline__ f2 df_from_double(double x) {
+  float h = (float)x;
+  float l = (float)(x - (double)h);
+  return {h, l};
+}
+
+__device__ __forceinline__ double df_to_double(f2 x) { return (double)x.h + (double)x.l; }
+
+// ------------------------------------------------------------------ slicing
+// Scale exponent of a group maximum: smallest e with max < 2^e (0 for 0).
+__device__ __forceinline__ int scale_exp(float mx) {
+  if (!(mx > 0.0f)) return 0;
+  int e;
+  frexpf(mx, &e);   // mx = f * 2^e, f in [0.5, 1)
+  return e;
+}
+
+// Write the 7 natural-weight digits of v = (h + l) * 2^(8 - e) to slices.
+__device__ __forceinline__ void slice_value(f2 v, int e, __nv_bfloat16* out, int64_t plane,
+                                            int64_t off) {
+  float p = ldexpf(v.h, 8 - e), q = ldexpf(v.l, 8 - e);
+  float w = 1.0f;
+#pragma unroll
+  for (int i = 0; i < OZ_S; ++i) {
+    f2 s = two_sum(p, q);
+    float d = rintf(s.h);
+    out[i * plane + off] = __float2bfloat16_rn(d * w);
+    p = (s.h - d) * 256.0f;
+    q = s.l * 256.0f;
+    w *= 0.00390625f;
+  }
+}
+
+struct SliceSrc {
+  const double* d;     // FP64 source (mask applies), or nullptr
+  const float2* df;    // df64 source, or nullptr
+  int64_t ld;
+  int mask;            // kDense / kUnitLower / kUpper (FP64 source)
+  int64_t off;         // diagonal offset of the mask
+};
+
+__device__ __forceinline__ f2 src_at(const SliceSrc& s, int64_t r, int64_t c) {
+  if (s.df) {
+    float2 v = s.df[c * s.ld + r];
+    return {v.x, v.y};
+  }
+  double x;
+  switch (s.mask) {
+    case kUnitLower: x = (r > c + s.off) ? s.d[c * s.ld + r] : (r == c + s.off ? 1.0 : 0.0); break;
+    case kUpper: x = (r <= c + s.off) ? s.d[c * s.ld + r] : 0.0; break;
+    default: x = s.d[c * s.ld + r];
+  }
+  return df_from_double(x);
+}
+
+// Operand element (n, k) = src(k, n): K runs down the columns of a column-major
+// source (rows k0 .. k0 + K).  One warp per (n, K group of G); n in [0, Nvalid)
+// are data, rows beyond are zero padding up to Rpad; k beyond Kvalid are zero.
+// Slices: OZ_S planes of Rpad x Kpad (cm order); exponents e[(k/G) * Rpad + n].
+__global__ void k_slice_kcol(SliceSrc src, int64_t k0, int64_t Kvalid, int64_t Nvalid, int64_t Rpad,
+                             int64_t Kpad, int G, __nv_bfloat16* out, int* eout) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t ngroups = Kpad / G;
+  if (wid >= Rpad * ngroups) return;
+  const int64_t n = wid % Rpad, g = wid / Rpad;
+  const int64_t plane = Rpad * Kpad;
+  float mx = 0.0f;
+  if (n < Nvalid) {
+    for (int64_t k = g * G + lane; k < (g + 1) * G && k < Kvalid; k += 32) {
+      f2 v = src_at(src, k0 + k, n);
+      mx = fmaxf(mx, fabsf(v.h));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  // the lo part can push |x| just above |hi|'s bound; leave one ulp of room
+  const int e = scale_exp(mx * (1.0f + 1.0e-6f));
+  if (lane == 0) eout[g * Rpad + n] = e;
+  for (int64_t k = g * G + lane; k < (g + 1) * G; k += 32) {
+    f2 v = {0.0f, 0.0f};
+    if (n < Nvalid && k < Kvalid) v = src_at(src, k0 + k, n);
+    slice_value(v, e, out, plane, cm_off(n, k, Rpad));
+  }
+}
+
+// Operand element (n, k) = src(n, k): K runs along the rows of a column-major
+// source (rows n0 + n, columns 0 .. K).  Scale group = the whole row (G = Kpad).
+// A CTA stages 32 rows x Kpad columns through shared memory.
+__global__ void k_slice_krow(SliceSrc src, int64_t n0, int64_t Nvalid, int64_t Kvalid, int64_t Rpad,
+                             int64_t Kpad, __nv_bfloat16* out, int* eout) {
+  extern __shared__ float2 tile[];   // [32][Kpad]
+  const int64_t nb = (int64_t)blockIdx.x * 32;
+  for (int64_t idx = threadIdx.x; idx < 32 * Kpad; idx += blockDim.x) {
+    int64_t rr = idx % 32, k = idx / 32;
+    int64_t n = nb + rr;
+    f2 v = {0.0f, 0.0f};
+    if (n < Nvalid && k < Kvalid) v = src_at(src, n0 + n, k);
+    tile[rr * Kpad + k] = make_float2(v.h, v.l);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int64_t plane = Rpad * Kpad;
+  for (int rr = warp; rr < 32; rr += nw) {
+    const int64_t n = nb + rr;
+    if (n >= Rpad) continue;
+    float mx = 0.0f;
+    for (int64_t k = lane; k < Kpad; k += 32) mx = fmaxf(mx, fabsf(tile[rr * Kpad + k].x));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const int e = scale_exp(mx * (1.0f + 1.0e-6f));
+    if (lane == 0) eout[n] = e;
+    for (int64_t k = lane; k < Kpad; k += 32) {
+      float2 t = tile[rr * Kpad + k];
+      slice_value({t.x, t.y}, e, out, plane, cm_off(n, k, Rpad));
+    }
+  }
+}
+
+// ------------------------------------------------------------------ tcgen05 kernel
+struct OzArgs {
+  const __nv_bfloat16* As;   // A-operand slices: OZ_S planes of AR x Kpad
+  int64_t AR;
+  const __nv_bfloat16* Bs;   // B-operand slices: OZ_S planes of BR x Kpad
+  int64_t BR;
+  int64_t Kpad;              // multiple of 16
+  int64_t k_per_cta;         // K extent of one CTA (multiple of kgroup)
+  int64_t kgroup;            // K rows per scale group / accumulator readout
+  const int* eA;             // [Kpad / kgroup][AR]
+  const int* eB;             // [Kpad / kgroup][BR]
+  int mode;                  // 0: partial sums (df64) over the CTA's K range; 1: C -= product
+  float2* part;              // mode 0: [split][Nvalid][AR] (ld AR per column)
+  float2* C;                 // mode 1: df64 matrix (ld ldc)
+  double* C64;               // mode 1: same storage viewed as FP64
+  int64_t ldc;
+  int64_t Mvalid, Nvalid;
+  int64_t fp64_rows;         // mode 1: rows < fp64_rows are written as FP64 (final)
+  int* status;
+};
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+  for (long it = 0; it < OZ_WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  // K-major, no swizzle: LBO = 128 B (next 8 K elements), SBO = 256 B (next 8 rows)
+  return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) |
+         ((uint64_t)(256 >> 4) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void* g) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(g) : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs a) {
+  extern __shared__ __align__(1024) unsigned char oz_smem[];
+  __shared__ __align__(8) uint64_t mbar[OZ_STAGES];
+  __shared__ uint32_t tmem_base_s;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  unsigned char* ring = (unsigned char*)(((uintptr_t)oz_smem + 1023) & ~(uintptr_t)1023);
+
+  const int64_t m0 = (int64_t)blockIdx.x * OZ_M;
+  const int64_t n0 = (int64_t)blockIdx.y * OZ_N;
+  const int64_t kbeg = (int64_t)blockIdx.z * a.k_per_cta;
+  const int64_t kend = (kbeg + a.k_per_cta < a.Kpad) ? kbeg + a.k_per_cta : a.Kpad;
+  const int nsteps = (int)((kend - kbeg) / 16);
+  const int steps_per_group = (int)(a.kgroup / 16);
+
+  if (tid == 0) {
+    for (int s = 0; s < OZ_STAGES; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[s])));
+    s_fail = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_s)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base_s;
+
+  // loader: K16 step t into stage t % OZ_STAGES
+  auto load_step = [&](int t) {
+    const int st = t % OZ_STAGES;
+    const int64_t kb = (kbeg >> 4) + t;   // K16 block index
+    unsigned char* sbase = ring + (size_t)st * OZ_STAGE_BYTES;
+    // A: OZ_S slices x 4096 B; B: OZ_S slices x 3072 B, 16 B per copy
+    constexpr int ACH = OZ_ABYTES / 16, BCH = OZ_BBYTES / 16;
+    for (int idx = tid; idx < OZ_S * (ACH + BCH); idx += kThreads) {
+      int s, c;
+      const unsigned char* g;
+      uint32_t dst;
+      if (idx < OZ_S * ACH) {
+        s = idx / ACH;
+        c = idx % ACH;
+        g = (const unsigned char*)(a.As + s * a.AR * a.Kpad + kb * a.AR * 16 + (m0 >> 3) * 128) + c * 16;
+        dst = smem_u32(sbase + s * OZ_ABYTES + c * 16);
+      } else {
+        int j = idx - OZ_S * ACH;
+        s = j / BCH;
+        c = j % BCH;
+        g = (const unsigned char*)(a.Bs + s * a.BR * a.Kpad + kb * a.BR * 16 + (n0 >> 3) * 128) + c * 16;
+        dst = smem_u32(sbase + OZ_S * OZ_ABYTES + s * OZ_BBYTES + c * 16);
+      }
+      cp_async16(dst, g);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_N >> 3) << 17) |
+                         ((uint32_t)(OZ_M >> 4) << 24);
+  // df64 accumulators of mode 0: this thread's row, 48 columns (half of the tile)
+  const int q = warp & 3;            // TMEM lane quarter
+  const int half = warp >> 2;        // column half
+  const int row = q * 32 + lane;
+  f2 acc[48];
+#pragma unroll
+  for (int j = 0; j < 48; ++j) acc[j] = {0.0f, 0.0f};
+
+  for (int t = 0; t < OZ_STAGES - 1 && t < nsteps; ++t) load_step(t);
+  // MMA completion is tracked by thread 0 alone, in step order: step u is the
+  // (u / OZ_STAGES)-th commit on stage u % OZ_STAGES.
+  int next_done = 0;
+  auto ensure_done = [&](int u) -> bool {
+    for (; next_done <= u; ++next_done) {
+      if (!mbar_wait(smem_u32(&mbar[next_done % OZ_STAGES]), (uint32_t)((next_done / OZ_STAGES) & 1)))
+        return false;
+    }
+    return true;
+  };
+  int last_issued = -1;
+  for (int t = 0; t < nsteps; ++t) {
+    const int st = t % OZ_STAGES;
+    // the loads of step t are in the oldest outstanding group
+    if (t + 1 < nsteps)
+      asm volatile("cp.async.wait_group %0;" ::"n"(OZ_STAGES - 2) : "memory");
+    else
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    const int step_in_group = t % steps_per_group;
+    const bool group_end = (step_in_group == steps_per_group - 1) || (t == nsteps - 1);
+    const int refill = (t + OZ_STAGES - 1 < nsteps) ? t + OZ_STAGES - 1 : -1;
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      unsigned char* sbase = ring + (size_t)st * OZ_STAGE_BYTES;
+      bool first_of_group[OZ_G];
+#pragma unroll
+      for (int g = 0; g < OZ_G; ++g) first_of_group[g] = (step_in_group == 0);
+#pragma unroll
+      for (int i = 0; i < OZ_S; ++i) {
+#pragma unroll
+        for (int j = 0; j < OZ_S; ++j) {
+          if (i + j >= OZ_S) continue;
+          const int g = (i + j < OZ_G - 1) ? i + j : OZ_G - 1;
+          const uint64_t ad = make_desc(smem_u32(sbase + i * OZ_ABYTES));
+          const uint64_t bd = make_desc(smem_u32(sbase + OZ_S * OZ_ABYTES + j * OZ_BBYTES));
+          const uint32_t dt = tmem + (uint32_t)(g * OZ_N);
+          const uint32_t accum = first_of_group[g] ? 0u : 1u;
+          first_of_group[g] = false;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+        }
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&mbar[st]))
+          : "memory");
+      last_issued = t;
+      bool good = true;
+      // the stage refilled next was read by step t-1; step t's MMAs keep the pipe busy meanwhile
+      if (refill >= 0 && t >= 1) good = ensure_done(t - 1);
+      if (good && group_end) good = ensure_done(t);
+      if (!good) s_fail = 1;
+    }
+    __syncthreads();
+    if (s_fail) break;
+    if (refill >= 0) load_step(refill);
+    if (group_end) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int64_t grp = (kbeg + (int64_t)t * 16) / a.kgroup;
+      const int64_t gm = m0 + row;
+      const int eA = (gm < a.AR) ? a.eA[grp * a.AR + gm] : 0;
+#pragma unroll
+      for (int c16 = 0; c16 < 3; ++c16) {
+        const int cbase = half * 48 + c16 * 16;
+        float gv[OZ_G][16];
+#pragma unroll
+        for (int g = 0; g < OZ_G; ++g)
+          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * OZ_N + cbase), gv[g]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int64_t gn = n0 + cbase + j;
+          const int eB = (gn < a.BR) ? a.eB[grp * a.BR + gn] : 0;
+          f2 sv = two_sum(gv[0][j], gv[1][j]);
+          sv = fast_two_sum(sv.h, sv.l);
+          sv = df_add_f(sv, gv[2][j]);
+          sv = df_add_f(sv, gv[3][j]);
+          sv = df_add_f(sv, gv[4][j]);
+          const int sh = eA + eB - 16;
+          sv.h = ldexpf(sv.h, sh);
+          sv.l = ldexpf(sv.l, sh);
+          if (a.mode == 0) {
+            acc[c16 * 16 + j] = df_add(acc[c16 * 16 + j], sv);
+          } else if (gm < a.Mvalid && gn < a.Nvalid) {
+            const int64_t ci = gn * a.ldc + gm;
+            const float2 c = a.C[ci];
+            f2 r = df_add({c.x, c.y}, {-sv.h, -sv.l});
+            if (gm < a.fp64_rows) a.C64[ci] = df_to_double(r);
+            else a.C[ci] = make_float2(r.h, r.l);
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+    }
+  }
+  if (s_fail) {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (tid == 0) {
+      atomicExch(a.status, CANDMC_ERR_TIMEOUT);
+      // let in-flight MMAs finish (bounded) before TMEM is released
+      if (last_issued >= 0) ensure_done(last_issued);
+    }
+  } else if (a.mode == 0) {
+    const int64_t gm = m0 + row;
+    float2* out = a.part + (int64_t)blockIdx.z * a.Nvalid * a.AR;
+    if (gm < a.AR) {
+#pragma unroll
+      for (int j = 0; j < 48; ++j) {
+        const int64_t gn = n0 + half * 48 + j;
+        if (gn < a.Nvalid) out[gn * a.AR + gm] = make_float2(acc[j].h, acc[j].l);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
+// ------------------------------------------------------------------ conversions and reduction
+__global__ void k_to_df64(double* X, int64_t ld, int64_t m, int64_t n) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= m * n) return;
+  int64_t i = idx % m, j = idx / m;
+  double* p = X + j * ld + i;
+  f2 v = df_from_double(*p);
+  *reinterpret_cast<float2*>(p) = make_float2(v.h, v.l);
+}
+
+__global__ void k_from_df64(double* X, int64_t ld, int64_t m, int64_t n) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= m * n) return;
+  int64_t i = idx % m, j = idx / m;
+  double* p = X + j * ld + i;
+  float2 v = *reinterpret_cast<float2*>(p);
+  *p = (double)v.x + (double)v.y;
+}
+
+// Z (nb x n, FP64, ld nb) = sum over splits of the df64 partials [split][n][AR].
+__global__ void k_oz_sum_partials(const float2* part, int nsplit, int64_t AR, int nb, int64_t n,
+                                  double* Z) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)nb * n) return;
+  int64_t i = idx % nb, j = idx / nb;
+  f2 s = {0.0f, 0.0f};
+  for (int sp = 0; sp < nsplit; ++sp) {
+    float2 v = part[(int64_t)sp * n * AR + j * AR + i];
+    s = df_add(s, {v.x, v.y});
+  }
+  Z[j * nb + i] = df_to_double(s);
+}
+
+// ------------------------------------------------------------------ host side
+static inline int64_t rup(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+static int num_sms_oz() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 148;
+  }
+  return n;
+}
+
+int to_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return CANDMC_OK;
+  ProfScope ps(CANDMC_KCLASS_OZ_SLICE, 16.0 * m * n, s);
+  k_to_df64<<<(unsigned)((m * n + 255) / 256), 256, 0, s>>>(X, ld, m, n);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+int from_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return CANDMC_OK;
+  ProfScope ps(CANDMC_KCLASS_OZ_SLICE, 16.0 * m * n, s);
+  k_from_df64<<<(unsigned)((m * n + 255) / 256), 256, 0, s>>>(X, ld, m, n);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+static int launch_slice_kcol(SliceSrc src, int64_t k0, int64_t Kvalid, int64_t Nvalid, int64_t Rpad,
+                             int64_t Kpad, int G, __nv_bfloat16* out, int* e, cudaStream_t s) {
+  int64_t warps = Rpad * (Kpad / G);
+  ProfScope ps(CANDMC_KCLASS_OZ_SLICE, 8.0 * Nvalid * Kvalid + 14.0 * Rpad * Kpad, s);
+  k_slice_kcol<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(src, k0, Kvalid, Nvalid, Rpad,
+                                                                      Kpad, G, out, e);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+static int launch_slice_krow(SliceSrc src, int64_t n0, int64_t Nvalid, int64_t Kvalid, int64_t Rpad,
+                             int64_t Kpad, __nv_bfloat16* out, int* e, cudaStream_t s) {
+  size_t sm = sizeof(float2) * 32 * (size_t)Kpad;
+  if (sm > 48 * 1024)
+    CANDMC_CK(cudaFuncSetAttribute(k_slice_krow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  ProfScope ps(CANDMC_KCLASS_OZ_SLICE, 8.0 * Nvalid * Kvalid + 14.0 * Rpad * Kpad, s);
+  k_slice_krow<<<(unsigned)((Rpad + 31) / 32), 256, sm, s>>>(src, n0, Nvalid, Kvalid, Rpad, Kpad, out, e);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+static int launch_oz(const OzArgs& a, unsigned gm, unsigned gn, unsigned gk, int cls, double flops,
+                     cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    CANDMC_CK(cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
+    attr = true;
+  }
+  ProfScope ps(cls, flops, s);
+  k_oz_mma<<<dim3(gm, gn, gk), kThreads, OZ_SMEM, s>>>(a);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+// Trailing update in the emulated-FP64 form.  C (m x n, ld ldc) holds df64
+// pairs; rows < fp64_rows of C are written back as FP64 (finished R rows).
+// Y: unit-lower m x nb (read from a Y\R buffer, FP64), T: nb x nb upper.
+int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
+                   double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
+                   cudaStream_t s) {
+  if (m <= 0 || n <= 0) return CANDMC_OK;
+  if (nb > OZ_M) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
+  const int64_t KG = 128;                       // K rows per exact accumulation
+  // ---- GEMM1: Z = Y^T C.  A-op = Y^T (rows = Householder index, K = m), B-op = C (rows = columns)
+  const int64_t Kp1 = rup(m, KG);
+  const int64_t AR1 = OZ_M, BR1 = rup(n, OZ_N);
+  DevBuf ya, ea, cb, eb, part, z;
+  CANDMC_RET(ya.alloc(sizeof(__nv_bfloat16) * OZ_S * AR1 * Kp1, s));
+  CANDMC_RET(ea.alloc(sizeof(int) * (Kp1 / KG) * AR1, s));
+  CANDMC_RET(cb.alloc(sizeof(__nv_bfloat16) * OZ_S * BR1 * Kp1, s));
+  CANDMC_RET(eb.alloc(sizeof(int) * (Kp1 / KG) * BR1, s));
+  SliceSrc ysrc{Y, nullptr, ldy, ymask, 0};
+  auto* yas = static_cast<__nv_bfloat16*>(ya.p);
+  auto* cbs = static_cast<__nv_bfloat16*>(cb.p);
+  CANDMC_RET(launch_slice_kcol(ysrc, 0, m, nb, AR1, Kp1, (int)KG, yas, static_cast<int*>(ea.p), s));
+  SliceSrc csrc{nullptr, reinterpret_cast<const float2*>(C), ldc, kDense, 0};
+  CANDMC_RET(launch_slice_kcol(csrc, 0, m, n, BR1, Kp1, (int)KG, cbs, static_cast<int*>(eb.p), s));
+  // K split: about two waves of CTAs
+  const int64_t ntiles = BR1 / OZ_N;
+  int64_t ksplit = std::max<int64_t>(1, std::min<int64_t>(Kp1 / KG, (2 * num_sms_oz() + ntiles - 1) / ntiles));
+  int64_t kper = rup((Kp1 + ksplit - 1) / ksplit, KG);
+  ksplit = (Kp1 + kper - 1) / kper;
+  CANDMC_RET(part.alloc(sizeof(float2) * ksplit * n * AR1, s));
+  OzArgs g1{};
+  g1.As = yas; g1.AR = AR1; g1.Bs = cbs; g1.BR = BR1; g1.Kpad = Kp1; g1.k_per_cta = kper;
+  g1.kgroup = KG; g1.eA = static_cast<int*>(ea.p); g1.eB = static_cast<int*>(eb.p);
+  g1.mode = 0; g1.part = static_cast<float2*>(part.p); g1.Mvalid = nb; g1.Nvalid = n;
+  g1.status = status;
+  CANDMC_RET(launch_oz(g1, 1, (unsigned)ntiles, (unsigned)ksplit, CANDMC_KCLASS_OZ_TN,
+                       2.0 * nb * n * m, s));
+  // ---- Z' = T^T * sum(partials)   (FP64, nb x n)
+  CANDMC_RET(z.alloc(sizeof(double) * nb * n, s));
+  DevBuf zt;
+  CANDMC_RET(zt.alloc(sizeof(double) * nb * n, s));
+  {
+    ProfScope ps(CANDMC_KCLASS_REDUCE, 8.0 * ksplit * n * AR1, s);
+    k_oz_sum_partials<<<(unsigned)((nb * n + 255) / 256), 256, 0, s>>>(
+        static_cast<float2*>(part.p), (int)ksplit, AR1, nb, n, z.d());
+    CANDMC_CK(cudaGetLastError());
+  }
+  CANDMC_RET(small_gemm(nb, n, nb, 1.0, Top, mref(z.d(), nb), 0.0, zt.d(), nb, s));
+  // ---- GEMM2: C -= Y * Z'.  A-op = Y (rows = m, K = nb), B-op = Z'^T (rows = columns, K = nb)
+  const int64_t Kp2 = rup(nb, 16);
+  const int64_t AR2 = rup(m, OZ_M), BR2 = rup(n, OZ_N);
+  DevBuf y2, ey2, z2, ez2;
+  CANDMC_RET(y2.alloc(sizeof(__nv_bfloat16) * OZ_S * AR2 * Kp2, s));
+  CANDMC_RET(ey2.alloc(sizeof(int) * AR2, s));
+  CANDMC_RET(z2.alloc(sizeof(__nv_bfloat16) * OZ_S * BR2 * Kp2, s));
+  CANDMC_RET(ez2.alloc(sizeof(int) * BR2, s));
+  CANDMC_RET(launch_slice_krow(ysrc, 0, m, nb, AR2, Kp2, static_cast<__nv_bfloat16*>(y2.p),
+                               static_cast<int*>(ey2.p), s));
+  SliceSrc zsrc{zt.d(), nullptr, nb, kDense, 0};
+  CANDMC_RET(launch_slice_kcol(zsrc, 0, nb, n, BR2, Kp2, (int)Kp2, static_cast<__nv_bfloat16*>(z2.p),
+                               static_cast<int*>(ez2.p), s));
+  OzArgs g2{};
+  g2.As = static_cast<__nv_bfloat16*>(y2.p); g2.AR = AR2;
+  g2.Bs = static_cast<__nv_bfloat16*>(z2.p); g2.BR = BR2;
+  g2.Kpad = Kp2; g2.k_per_cta = Kp2; g2.kgroup = Kp2;
+  g2.eA = static_cast<int*>(ey2.p); g2.eB = static_cast<int*>(ez2.p);
+  g2.mode = 1; g2.C = reinterpret_cast<float2*>(C); g2.C64 = C; g2.ldc = ldc;
+  g2.Mvalid = m; g2.Nvalid = n; g2.fp64_rows = fp64_rows; g2.status = status;
+  CANDMC_RET(launch_oz(g2, (unsigned)(AR2 / OZ_M), (unsigned)(BR2 / OZ_N), 1, CANDMC_KCLASS_OZ_NN,
+                       2.0 * m * n * nb, s));
+  return CANDMC_OK;
+}
+
+}  // namespace candmc
