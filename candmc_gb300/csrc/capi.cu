@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <string>
+#include <vector>
 
 #include "kernels.cuh"
 
@@ -89,7 +90,7 @@ int apply_qt(const double* Y, int64_t ldy, int64_t m, int nb, const double* T, i
 // upper-triangular factor; the strictly lower part of T is zeroed.
 static int hr_rec(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, int* st,
                   int precision, cudaStream_t s) {
-  if (b <= kDirectB) return hr_direct(A, lda, m, b, T, ldT, nullptr, 0, st, s);
+  if (b <= kDirectB) return hr_direct4(A, lda, m, b, T, ldT, nullptr, 0, st, s);
   const int b1 = b / 2, b2 = b - b1;
   CANDMC_RET(hr_rec(A, lda, m, b1, T, ldT, st, precision, s));
   // the panel itself stays in FP64 (its updates are m x b/2 x b/2: small)
@@ -131,7 +132,7 @@ static int hh_recon_dev(double* A, int64_t lda, int64_t m, int64_t b, double* W,
     T = tb.d();
     ldT = b;
   }
-  if (b <= kDirectB) return hr_direct(A, lda, m, (int)b, T, ldT, W, ldW, st, s);
+  if (b <= kDirectB) return hr_direct4(A, lda, m, (int)b, T, ldT, W, ldW, st, s);
   CANDMC_RET(hr_rec(A, lda, m, (int)b, T, ldT, st, precision, s));
   if (W) {
     CANDMC_RET(small_gemm(b, b, b, -1.0, mref(T, ldT, 0, kUpper), mref(A, lda, 1, kUnitLower), 0.0,
@@ -188,6 +189,120 @@ static int upd_core(const double* Y, int64_t ldy, int ymask, double* A, int64_t 
   CANDMC_RET(gemm_tn_reduce(Ym, mref(A, lda), mb, (int)b, kb, mref(top.d(), b, 0, kLower), 1.0,
                             z.d(), b, s));
   CANDMC_RET(gemm_nn_sub(A, lda, Ym, z.d(), b, mb, kb, (int)b, s));
+  return CANDMC_OK;
+}
+
+// Trailing update of columns [c0, c0 + n) of the block whose panel starts at P
+// (Y in P's Y\R, T upper), in the requested arithmetic.  In the emulated form
+// the columns hold df64 pairs and their top b rows are written back as FP64.
+static int update_cols(double* P, int64_t lda, int64_t mm, int64_t b, const double* T, int64_t c0,
+                       int64_t n, int* st, int precision, cudaStream_t s) {
+  if (n <= 0) return CANDMC_OK;
+  double* C = P + c0 * lda;
+  if (precision == CANDMC_PREC_OZAKI)
+    return apply_qt_ozaki(P, lda, kUnitLower, mm, (int)b, mref(T, b, 1, kUpper), C, lda, n, b, st, s);
+  return apply_qt(P, lda, mm, (int)b, T, b, C, lda, n, precision, s);
+}
+
+// High-priority, non-blocking side stream per device for the lookahead panels.
+static cudaStream_t panel_stream() {
+  static cudaStream_t sp[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!sp[dev]) {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&sp[dev], cudaStreamNonBlocking, hi) != cudaSuccess)
+      sp[dev] = nullptr;
+  }
+  return sp[dev];
+}
+
+struct EventRing {
+  std::vector<cudaEvent_t> ev;
+  ~EventRing() {
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+  int make(cudaEvent_t* out) {
+    cudaEvent_t e;
+    CANDMC_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ev.push_back(e);
+    *out = e;
+    return CANDMC_OK;
+  }
+};
+
+// QR_2D_pipe on one GPU (alg/QR/qr_2d/qr_2d.cxx:378-635): the lookahead
+// pipeline of the reference, with the process columns replaced by two
+// streams.  Panel i+1 is factored on a high-priority side stream while the
+// bulk of panel i's trailing update runs on the caller's stream:
+//   side: HR(i); wait(A_{i-1}); U_next(i) = Q_i^T on panel i+1's columns; HR(i+1) ...
+//   main: wait(HR(i)); A_i = Q_i^T on panel i+2's columns (recorded); Q_i^T on the rest
+// Every column block receives Q_0^T .. Q_{i}^T in order, so the result is the
+// same factorization as QR_2D.
+static int qr_2d_pipe_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int* st,
+                          int precision, cudaStream_t s) {
+  const bool oz = (precision == CANDMC_PREC_OZAKI);
+  if (precision != CANDMC_PREC_FP64 && !oz) return set_error(CANDMC_ERR_ARG, "precision form not built");
+  if (oz && b > 128) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
+  cudaStream_t sp = panel_stream();
+  if (!sp) return set_error(CANDMC_ERR_CUDA, "could not create the lookahead stream");
+  EventRing evs;
+  DevBuf tbuf;   // ring of three T factors
+  CANDMC_RET(tbuf.alloc(sizeof(double) * 3 * b * b, s));
+  cudaEvent_t e_start;
+  CANDMC_RET(evs.make(&e_start));
+  if (oz) CANDMC_RET(to_df64(A, lda, m, k, s));
+  CANDMC_CK(cudaEventRecord(e_start, s));
+  CANDMC_CK(cudaStreamWaitEvent(sp, e_start, 0));
+  const int64_t npan = (k + b - 1) / b;
+  cudaEvent_t e_prevA = nullptr;   // main stream finished Q_{i-1}^T on panel i+1's columns
+  // panel 0 on the side stream
+  {
+    const int64_t bb = std::min(k, b);
+    if (oz) CANDMC_RET(from_df64(A, lda, m, bb, sp));
+    CANDMC_RET(hr_rec(A, lda, m, (int)bb, tbuf.d(), b, st, precision, sp));
+  }
+  for (int64_t i = 0; i < npan; ++i) {
+    const int64_t r0 = i * b, mm = m - r0, kk = k - r0;
+    double* P = A + r0 * lda + r0;
+    double* Ti = tbuf.d() + (i % 3) * b * b;
+    const bool trailing = (kk - b > 0 && mm - b > 0);
+    cudaEvent_t e_hr;
+    CANDMC_RET(evs.make(&e_hr));
+    CANDMC_CK(cudaEventRecord(e_hr, sp));   // HR(i) done (it was issued on sp)
+    if (!trailing) break;
+    // side stream: next panel's columns, then its factorization
+    const int64_t nnext = std::min(b, kk - b);
+    if (e_prevA) CANDMC_CK(cudaStreamWaitEvent(sp, e_prevA, 0));
+    CANDMC_RET(update_cols(P, lda, mm, b, Ti, b, nnext, st, precision, sp));
+    {
+      const int64_t r1 = r0 + b;
+      double* P1 = A + r1 * lda + r1;
+      const int64_t bb1 = std::min(k - r1, b);
+      double* T1 = tbuf.d() + ((i + 1) % 3) * b * b;
+      if (oz) CANDMC_RET(from_df64(P1, lda, m - r1, bb1, sp));
+      CANDMC_RET(hr_rec(P1, lda, m - r1, (int)bb1, T1, b, st, precision, sp));
+    }
+    // main stream: Q_i^T on panel i+2's columns (recorded), then the rest
+    CANDMC_CK(cudaStreamWaitEvent(s, e_hr, 0));
+    const int64_t na = std::min(b, std::max<int64_t>(0, kk - 2 * b));
+    if (na > 0) {
+      CANDMC_RET(update_cols(P, lda, mm, b, Ti, 2 * b, na, st, precision, s));
+      cudaEvent_t ea;
+      CANDMC_RET(evs.make(&ea));
+      CANDMC_CK(cudaEventRecord(ea, s));
+      e_prevA = ea;
+    } else {
+      e_prevA = nullptr;
+    }
+    CANDMC_RET(update_cols(P, lda, mm, b, Ti, 3 * b, kk - 3 * b, st, precision, s));
+  }
+  // the caller's stream waits for the side stream's last work
+  cudaEvent_t e_end;
+  CANDMC_RET(evs.make(&e_end));
+  CANDMC_CK(cudaEventRecord(e_end, sp));
+  CANDMC_CK(cudaStreamWaitEvent(s, e_end, 0));
   return CANDMC_OK;
 }
 
@@ -446,7 +561,8 @@ int candmc_QR_2D_host(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, i
     Status st;
     CANDMC_RET(st.init(s));
     CANDMC_RET(dA.in(A, lda, m, k, s));
-    CANDMC_RET(qr_2d_dev(dA.d.d(), dA.ldd, m, k, b, nullptr, 0, st.p(), precision, s));
+    // the lookahead pipeline: the same factorization as qr_2d_dev, panels overlapped
+    CANDMC_RET(qr_2d_pipe_dev(dA.d.d(), dA.ldd, m, k, b, st.p(), precision, s));
     CANDMC_RET(dA.out(A, lda, m, k, s));
     rc = st.check(s);
   }
@@ -486,7 +602,11 @@ int candmc_QR_2D_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int
 
 int candmc_QR_2D_pipe(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int precision,
                       void* stream) {
-  return candmc_QR_2D(A, lda, m, k, b, nullptr, 0, precision, stream);
+  if (!A || b < 1 || k < 1 || m < k || lda < m) return set_error(CANDMC_ERR_ARG, "QR_2D_pipe args");
+  cudaStream_t s = STREAM(stream);
+  Status st;
+  CANDMC_RET(st.init(s));
+  return qr_2d_pipe_dev(A, lda, m, k, b, st.p(), precision, s);
 }
 
 }  // extern "C"

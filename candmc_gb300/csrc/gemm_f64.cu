@@ -235,8 +235,10 @@ int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top,
   if (nb <= 0 || n <= 0) return CANDMC_OK;
   if (nb > 256) return CANDMC_ERR_ARG;
   const int64_t tiles = ((nb + TM - 1) / TM) * ((n + TN - 1) / TN);
-  const int64_t target = 2 * (int64_t)num_sms();
-  int64_t nsplit = std::max<int64_t>(1, std::min<int64_t>((target + tiles - 1) / tiles, (m + 255) / 256));
+  // FP64 work per CTA is what bounds these kernels: aim at ~4 CTAs per SM,
+  // with slices of at least 64 rows
+  const int64_t target = 4 * (int64_t)num_sms();
+  int64_t nsplit = std::max<int64_t>(1, std::min<int64_t>((target + tiles - 1) / tiles, (m + 63) / 64));
   nsplit = std::min<int64_t>(nsplit, 1024);
   int64_t kchunk = (m + nsplit - 1) / nsplit;
   kchunk = ((kchunk + TK - 1) / TK) * TK;

@@ -21,9 +21,13 @@ class ProfScope {
   cudaEvent_t e0_{}, e1_{};
 };
 
-// panel.cu: direct TSQR-HR of an m x b panel, b <= kDirectB.
+// panel.cu: direct TSQR-HR of an m x b panel, b <= kDirectB (binary tree,
+// explicit Q factors; used by the fixed-scratch entry point).
 int hr_direct(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
               int64_t ldW, int* d_status, cudaStream_t s);
+// tsqr4.cu: direct TSQR-HR with a fan-in-4 tree and compact-WY Q blocks.
+int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
+               int64_t ldW, int* d_status, cudaStream_t s);
 
 // gemm_f64.cu
 int small_gemm(int64_t M, int64_t N, int64_t K, double alpha, MatRef A, MatRef B, double beta,

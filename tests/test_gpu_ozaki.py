@@ -100,6 +100,25 @@ def test_QR_2D_ozaki_ill_conditioned(cm):
     assert np.linalg.norm(R1 - R2) / np.linalg.norm(R2) <= 1e-12
 
 
+@pytest.mark.parametrize("m,k,b,prec", [(1000, 700, 128, "ozaki"), (777, 777, 64, "ozaki"),
+                                        (600, 450, 32, "fp64"), (1536, 1536, 128, "ozaki")])
+def test_QR_2D_pipe_lookahead(cm, m, k, b, prec):
+    """Lookahead pipeline (panel i+1 on a side stream during panel i's update)
+    computes the same factorization as QR_2D."""
+    A = fx.gaussian(m, k, 5 * m + k)
+    Ao = A.copy()
+    co.QR_2D(Ao, b)
+    dA = dev(A)
+    cm.QR_2D_pipe(dA, b, precision=prec)
+    torch.cuda.synchronize()
+    YR = host(dA)
+    D = np.abs(YR - Ao)
+    if m == k:
+        D[-1, -1] = abs(abs(YR[-1, -1]) - abs(Ao[-1, -1]))
+    assert D.max() <= 1e-10 * np.abs(Ao).max(), D.max()
+    assert co.backward_error(A, YR) <= BWD_TOL
+
+
 def test_QR_2D_ozaki_host_entry(cm):
     A = fx.gaussian(500, 400, 77)
     Ao = A.copy()
