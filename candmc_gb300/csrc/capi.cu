@@ -470,6 +470,21 @@ int candmc_construct_Q1(const double* Y, int64_t ldy, const double* tau, double*
   return CANDMC_OK;
 }
 
+int candmc_apply_tsqr_QT(const double* Y, int64_t ldy, const double* tau, double* B, int64_t ldb,
+                         int64_t m, int64_t b, int64_t k, void* stream) {
+  if (!Y || !tau || !B || b < 1 || m < b || ldy < m || ldb < m || k < 0)
+    return set_error(CANDMC_ERR_ARG, "apply_tsqr_QT args");
+  if (k == 0) return CANDMC_OK;
+  cudaStream_t s = STREAM(stream);
+  DevBuf g, t;
+  CANDMC_RET(g.alloc(sizeof(double) * b * b, s));
+  CANDMC_RET(t.alloc(sizeof(double) * b * b, s));
+  MatRef Ym = mref(Y, ldy, 0, kUnitLower);
+  CANDMC_RET(gemm_tn_reduce(Ym, Ym, m, (int)b, b, mref(nullptr, 0), 1.0, g.d(), b, s));
+  CANDMC_RET(larft_from_gram(g.d(), b, tau, (int)b, t.d(), b, s));
+  return apply_qt(Y, ldy, m, (int)b, t.d(), b, B, ldb, k, CANDMC_PREC_FP64, s);
+}
+
 int candmc_compute_invT_from_W(const double* W, int64_t b, double* invT, void* stream) {
   if (!W || !invT || b < 1) return set_error(CANDMC_ERR_ARG, "compute_invT_from_W args");
   cudaStream_t s = STREAM(stream);

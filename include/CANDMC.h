@@ -1,0 +1,22 @@
+/*
+ * CANDMC.h for the GB300 QR hot path: the QR part of the reference's
+ * umbrella header (include/CANDMC.h:19-32), with the single-GPU drop-in
+ * declarations.  The MM, LU, SE and Yamamoto parts of the reference are not
+ * provided by this library.
+ */
+#ifndef __CANDMC_H__
+#define __CANDMC_H__
+
+/* binary tree TSQR on panels of matrices */
+#include "candmc/bitree_tsqr.h"
+
+/* TSQR with Householder vector reconstruction */
+#include "candmc/hh_recon.h"
+
+/* 2D QR algorithms for full matrices */
+#include "candmc/qr_2d.h"
+
+/* the C ABI underneath */
+#include "candmc_gb300.h"
+
+#endif

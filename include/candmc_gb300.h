@@ -110,6 +110,13 @@ int candmc_bitree_tsqr(double* A, int64_t lda, double* R, double* tau, int64_t m
 int candmc_construct_Q1(const double* Y, int64_t ldy, const double* tau, double* Q1, int64_t ldq,
                         int64_t m, int64_t b, int64_t k, void* stream);
 
+/* apply_tsqr_QT at numPes == 1: alg/QR/tsqr/bitree_tsqr.h:126-138
+ * (apply_tsqr_QT.cxx:31-163 on one rank: dlarft + dlarfb, i.e. dormqr 'L','T').
+ * B (m x k, ld ldb) <- Q^T B with Q = H_0...H_{b-1} from the reflectors in Y
+ * (lower part of a Y\R buffer, m x b) and tau. */
+int candmc_apply_tsqr_QT(const double* Y, int64_t ldy, const double* tau, double* B, int64_t ldb,
+                         int64_t m, int64_t b, int64_t k, void* stream);
+
 /* compute_invT_from_W: alg/QR/hh_recon/hh_recon.h:13-15 (hh_recon.cxx:26-31).
  * invT (b x b, ld b) holds Y1 on entry and T^-T = -W^-T*Y1 on return. */
 int candmc_compute_invT_from_W(const double* W, int64_t b, double* invT, void* stream);

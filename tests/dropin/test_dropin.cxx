@@ -1,0 +1,133 @@
+// Reference-style driver for the C++ drop-in (include/CANDMC.h) on one GPU.
+//
+// Mirrors the reference's own QR tests: the decomposition-independent srand48
+// fixture (test/QR/test_hh_recon.cxx:70-85, test_qr_2d.cxx:87-103), the same
+// entry points with a single-rank CommData_t / 1 x 1 pview, and the same pass
+// criteria (sum_j ||(A - QR) e_j|| / ||A e_j|| <= 1e-9; ||Q^T Q - I|| <= 1e-6).
+// Q is applied with the drop-in's apply_tsqr_QT, tau is rebuilt from Y as the
+// reference's tau_recon does (alg/shared/util.cxx:437-466).  Prints
+// "Test successful." or "TEST FAILED!!!" per test and exits non-zero on a failure.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+
+#include <vector>
+
+#include "CANDMC.h"
+
+static double fixture(int64_t row, int64_t col, int64_t m, double shift) {
+  srand48(99900 + (row + col * m) * 61);
+  return drand48() - shift;
+}
+
+// tau_i = 2 / (1 + ||Y[i+1:, i]||^2), the reconstruction convention (tau = 2 for an empty tail)
+static std::vector<double> tau_from_y(const std::vector<double>& YR, int64_t m, int64_t b) {
+  std::vector<double> tau(b);
+  for (int64_t i = 0; i < b; ++i) {
+    double s = 0;
+    for (int64_t r = i + 1; r < m; ++r) s += YR[i * m + r] * YR[i * m + r];
+    tau[i] = 2.0 / (1.0 + s);
+  }
+  return tau;
+}
+
+// sum_j ||(Q^T A - R) e_j|| / ||A e_j|| over the first b columns (== the reference's ||A - QR|| form)
+static double column_residual(const std::vector<double>& A, const std::vector<double>& YR, int64_t m,
+                              int64_t b, int64_t ncols) {
+  std::vector<double> tau = tau_from_y(YR, m, b);
+  std::vector<double> B(A);
+  CommData_t c;
+  SET_COMM(MPI_COMM_WORLD, 0, 1, c);
+  apply_tsqr_QT(YR.data(), m, tau.data(), B.data(), m, m, b, ncols, 0, 1, 0, c);
+  double sum = 0;
+  for (int64_t j = 0; j < ncols; ++j) {
+    double num = 0, den = 0;
+    for (int64_t r = 0; r < m; ++r) {
+      const double rr = (r <= j) ? YR[j * m + r] : 0.0;
+      num += (B[j * m + r] - rr) * (B[j * m + r] - rr);
+      den += A[j * m + r] * A[j * m + r];
+    }
+    sum += sqrt(num / den);
+  }
+  return sum;
+}
+
+static int report(const char* name, double value, double bound) {
+  const bool ok = value <= bound && candmc_dropin_last_status() == CANDMC_OK;
+  printf("%s: %.3e (bound %.0e) %s\n", name, value, bound, ok ? "Test successful." : "TEST FAILED!!!");
+  return ok ? 0 : 1;
+}
+
+int main() {
+  int fails = 0;
+  CommData_t cdt;
+  SET_COMM(MPI_COMM_WORLD, 0, 1, cdt);
+  // test_hh_recon at np = 1: b = 17, m = 34 (defaults), plus a taller panel
+  for (int64_t mm : {34, 1700}) {
+    const int64_t m = mm, b = 17;
+    std::vector<double> A(m * b), W(b * b);
+    for (int64_t c = 0; c < b; ++c)
+      for (int64_t r = 0; r < m; ++r) A[c * m + r] = fixture(r, c, m, 0.0);
+    std::vector<double> YR(A);
+    hh_recon_qr(YR.data(), m, m, b, W.data(), 0, 1, 0, 0, cdt);
+    char name[64];
+    snprintf(name, sizeof name, "hh_recon_qr m=%ld b=%ld ||A-QR||", (long)m, (long)b);
+    fails += report(name, column_residual(A, YR, m, b, b), 1e-9);
+  }
+  // test_construct_tsqr_Q: bitree_tsqr + construct_Q1, ||Q^T Q - I||_F <= 1e-6
+  {
+    const int64_t m = 84, b = 21;
+    std::vector<double> A(m * b), R(b * b), tau(b), Q1(m * b);
+    for (int64_t c = 0; c < b; ++c)
+      for (int64_t r = 0; r < m; ++r) A[c * m + r] = fixture(r, c, m, 0.0);
+    bitree_tsqr(A.data(), m, R.data(), tau.data(), m, b, 0, 1, 0, 0, cdt, 1);
+    construct_Q1(A.data(), m, tau.data(), Q1.data(), m, m, b, b, 0, 1, 0, cdt);
+    double e = 0;
+    for (int64_t i = 0; i < b; ++i)
+      for (int64_t j = 0; j < b; ++j) {
+        double s = (i == j) ? -1.0 : 0.0;
+        for (int64_t r = 0; r < m; ++r) s += Q1[i * m + r] * Q1[j * m + r];
+        e += s * s;
+      }
+    fails += report("bitree_tsqr + construct_Q1 ||Q^TQ-I||", sqrt(e), 1e-6);
+  }
+  // test_qr_2d at a 1 x 1 grid with the pipelined variant (its default): drand48 - 0.5
+  for (int prec : {CANDMC_PREC_FP64, CANDMC_PREC_OZAKI}) {
+    const int64_t m = 256, k = 192, b = 64;
+    std::vector<double> A(m * k);
+    for (int64_t c = 0; c < k; ++c)
+      for (int64_t r = 0; r < m; ++r) A[c * m + r] = fixture(r, c, m, 0.5);
+    std::vector<double> YR(A);
+    pview pv = candmc_single_gpu_view();
+    candmc_dropin_set_precision(prec);
+    QR_2D_pipe(YR.data(), m, m, k, b, &pv);
+    // apply Q^T panel by panel with update_A (T from Y^T Y) and compare with R
+    std::vector<double> B(A);
+    for (int64_t r0 = 0; r0 < k; r0 += b) {
+      pview pv2 = candmc_single_gpu_view();
+      update_A(YR.data() + r0 * m + r0, m, B.data() + r0, m, m - r0, k, b, NULL, &pv2, NULL, 0);
+    }
+    double num = 0, den = 0;
+    for (int64_t c = 0; c < k; ++c)
+      for (int64_t r = 0; r < m; ++r) {
+        const double rr = (r <= c) ? YR[c * m + r] : 0.0;
+        num += (B[c * m + r] - rr) * (B[c * m + r] - rr);
+        den += A[c * m + r] * A[c * m + r];
+      }
+    char name[64];
+    snprintf(name, sizeof name, "QR_2D_pipe %s ||A-QR||/||A||", prec == CANDMC_PREC_FP64 ? "fp64" : "ozaki");
+    fails += report(name, sqrt(num / den), 1e-13);
+  }
+  candmc_dropin_set_precision(CANDMC_PREC_FP64);
+  // a grid larger than 1 x 1 is rejected without touching the data
+  {
+    pview pv = candmc_single_gpu_view();
+    pv.ccol.np = 2;
+    std::vector<double> A(64 * 64, 1.0);
+    QR_2D(A.data(), 64, 64, 64, 16, &pv, NULL, 0);
+    const bool ok = candmc_dropin_last_status() == CANDMC_ERR_ARG && A[5] == 1.0;
+    printf("2x1 grid rejected: %s\n", ok ? "Test successful." : "TEST FAILED!!!");
+    fails += ok ? 0 : 1;
+  }
+  return fails ? 1 : 0;
+}
