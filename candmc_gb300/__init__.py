@@ -23,7 +23,7 @@ from ._abi import CandmcError, check
 __all__ = [
     "CandmcError", "colmajor", "empty_colmajor", "hh_recon_qr", "bitree_tsqr", "construct_Q1",
     "compute_invT_from_W", "signed_NLU", "recursive_NLU", "compute_invT_from_Y",
-    "compute_invT_from_Y2", "upd_A", "update_A", "QR_2D", "QR_2D_2D", "QR_2D_pipe",
+    "compute_invT_from_Y2", "upd_A", "update_A", "QR_2D", "QR_2D_2D", "QR_2D_pipe", "ls_solve",
     "PRECISIONS", "lib",
 ]
 
@@ -226,6 +226,24 @@ def QR_2D(A, b, aggreg_Y=None, precision="fp64", stream=None):
     pg, ldg = _dev(aggreg_Y, "aggreg_Y") if aggreg_Y is not None else (None, 0)
     check(lib().candmc_QR_2D(pa, lda, m, k, b, pg, ldg, _prec(precision), _stream(stream)), "QR_2D")
     return A
+
+
+def ls_solve(A, B, b=128, precision="fp64", max_refine=20, tol=1e-15, stream=None):
+    """min ||A X - B||: CAQR in the given form, X0 = R^-1 Q^T B, FP64 refinement
+    (corrected semi-normal equations).  Returns (X, stats) with stats =
+    {"steps", "last_change", "first_change", "status"}."""
+    import ctypes
+    m, n = A.shape
+    nrhs = B.shape[1]
+    X = empty_colmajor(n, nrhs, A.device)
+    pa, lda = _dev(A, "A")
+    pb, ldb = _dev(B, "B")
+    px, ldx = _dev(X, "X")
+    st = (ctypes.c_double * 4)()
+    check(lib().candmc_ls_solve(pa, lda, m, n, pb, ldb, nrhs, px, ldx, b, _prec(precision),
+                                int(max_refine), float(tol), st, _stream(stream)), "ls_solve")
+    return X, {"steps": int(st[0]), "last_change": st[1], "first_change": st[2],
+               "status": int(st[3])}
 
 
 def QR_2D_2D(A, b, b_sub, aggreg_Y=None, precision="fp64", stream=None):

@@ -170,18 +170,21 @@ static int upd_core(const double* Y, int64_t ldy, int ymask, double* A, int64_t 
                     int64_t kb, int64_t b, const double* W, int W_is_T, int precision,
                     cudaStream_t s) {
   if (mb <= 0 || kb <= 0) return CANDMC_OK;
-  if (precision != CANDMC_PREC_FP64 && precision != CANDMC_PREC_OZAKI)
-    return set_error(CANDMC_ERR_ARG, "precision form not built");
+  if (precision != CANDMC_PREC_FP64 && precision != CANDMC_PREC_OZAKI && precision != CANDMC_PREC_FP32)
+    return set_error(CANDMC_ERR_ARG, "unknown precision form");
   DevBuf top, z;
   CANDMC_RET(top.alloc(sizeof(double) * b * b, s));
   CANDMC_RET(top_from_W(Y, ldy, mb, b, W, W_is_T, ymask, top.d(), s));
-  if (precision == CANDMC_PREC_OZAKI) {
-    if (b > 128) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
+  if (precision != CANDMC_PREC_FP64) {
+    if (b > 128) return set_error(CANDMC_ERR_ARG, "the ozaki and fp32 forms need b <= 128");
     Status st;
     CANDMC_RET(st.init(s));
     CANDMC_RET(to_df64(A, lda, mb, kb, s));
-    CANDMC_RET(apply_qt_ozaki(Y, ldy, ymask, mb, (int)b, mref(top.d(), b, 0, kLower), A, lda, kb, 0,
-                              st.p(), s));
+    if (precision == CANDMC_PREC_OZAKI)
+      CANDMC_RET(apply_qt_ozaki(Y, ldy, ymask, mb, (int)b, mref(top.d(), b, 0, kLower), A, lda, kb, 0,
+                                st.p(), s));
+    else
+      CANDMC_RET(apply_qt_f32(Y, ldy, ymask, mb, (int)b, mref(top.d(), b, 0, kLower), A, lda, kb, 0, s));
     return from_df64(A, lda, mb, kb, s);
   }
   CANDMC_RET(z.alloc(sizeof(double) * b * kb, s));
@@ -201,7 +204,17 @@ static int update_cols(double* P, int64_t lda, int64_t mm, int64_t b, const doub
   double* C = P + c0 * lda;
   if (precision == CANDMC_PREC_OZAKI)
     return apply_qt_ozaki(P, lda, kUnitLower, mm, (int)b, mref(T, b, 1, kUpper), C, lda, n, b, st, s);
+  if (precision == CANDMC_PREC_FP32)
+    return apply_qt_f32(P, lda, kUnitLower, mm, (int)b, mref(T, b, 1, kUpper), C, lda, n, b, s);
   return apply_qt(P, lda, mm, (int)b, T, b, C, lda, n, precision, s);
+}
+
+// The ozaki and fp32 forms keep the unfactored part as df64 pairs.
+static int check_form(int precision, int64_t b, bool* pair) {
+  *pair = (precision == CANDMC_PREC_OZAKI || precision == CANDMC_PREC_FP32);
+  if (precision != CANDMC_PREC_FP64 && !*pair) return set_error(CANDMC_ERR_ARG, "unknown precision form");
+  if (*pair && b > 128) return set_error(CANDMC_ERR_ARG, "the ozaki and fp32 forms need b <= 128");
+  return CANDMC_OK;
 }
 
 // High-priority, non-blocking side stream per device for the lookahead panels.
@@ -240,16 +253,16 @@ struct EventRing {
 //   main: wait(HR(i)); A_i = Q_i^T on panel i+2's columns (recorded); Q_i^T on the rest
 // Every column block receives Q_0^T .. Q_{i}^T in order, so the result is the
 // same factorization as QR_2D.
-static int qr_2d_pipe_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int* st,
-                          int precision, cudaStream_t s) {
-  const bool oz = (precision == CANDMC_PREC_OZAKI);
-  if (precision != CANDMC_PREC_FP64 && !oz) return set_error(CANDMC_ERR_ARG, "precision form not built");
-  if (oz && b > 128) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
+int qr_2d_pipe_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int* st, int precision,
+                   cudaStream_t s, double* Tall) {
+  bool oz;
+  CANDMC_RET(check_form(precision, b, &oz));
   cudaStream_t sp = panel_stream();
   if (!sp) return set_error(CANDMC_ERR_CUDA, "could not create the lookahead stream");
   EventRing evs;
-  DevBuf tbuf;   // ring of three T factors
-  CANDMC_RET(tbuf.alloc(sizeof(double) * 3 * b * b, s));
+  DevBuf tbuf;   // ring of three T factors, or every panel's T (Tall: b x b per panel)
+  if (!Tall) CANDMC_RET(tbuf.alloc(sizeof(double) * 3 * b * b, s));
+  auto tslot = [&](int64_t i) { return Tall ? Tall + i * b * b : tbuf.d() + (i % 3) * b * b; };
   cudaEvent_t e_start;
   CANDMC_RET(evs.make(&e_start));
   if (oz) CANDMC_RET(to_df64(A, lda, m, k, s));
@@ -261,12 +274,12 @@ static int qr_2d_pipe_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t 
   {
     const int64_t bb = std::min(k, b);
     if (oz) CANDMC_RET(from_df64(A, lda, m, bb, sp));
-    CANDMC_RET(hr_rec(A, lda, m, (int)bb, tbuf.d(), b, st, precision, sp));
+    CANDMC_RET(hr_rec(A, lda, m, (int)bb, tslot(0), b, st, precision, sp));
   }
   for (int64_t i = 0; i < npan; ++i) {
     const int64_t r0 = i * b, mm = m - r0, kk = k - r0;
     double* P = A + r0 * lda + r0;
-    double* Ti = tbuf.d() + (i % 3) * b * b;
+    double* Ti = tslot(i);
     const bool trailing = (kk - b > 0 && mm - b > 0);
     cudaEvent_t e_hr;
     CANDMC_RET(evs.make(&e_hr));
@@ -280,7 +293,7 @@ static int qr_2d_pipe_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t 
       const int64_t r1 = r0 + b;
       double* P1 = A + r1 * lda + r1;
       const int64_t bb1 = std::min(k - r1, b);
-      double* T1 = tbuf.d() + ((i + 1) % 3) * b * b;
+      double* T1 = tslot(i + 1);
       if (oz) CANDMC_RET(from_df64(P1, lda, m - r1, bb1, sp));
       CANDMC_RET(hr_rec(P1, lda, m - r1, (int)bb1, T1, b, st, precision, sp));
     }
@@ -310,12 +323,11 @@ static int qr_2d_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, do
                      int64_t lda_aY, int* st, int precision, cudaStream_t s) {
   DevBuf tb;
   CANDMC_RET(tb.alloc(sizeof(double) * b * b, s));
-  const bool oz = (precision == CANDMC_PREC_OZAKI);
-  if (precision != CANDMC_PREC_FP64 && !oz) return set_error(CANDMC_ERR_ARG, "precision form not built");
-  if (oz && b > 128) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
-  // emulated form: the not-yet-factored part lives as df64 pairs; each panel is
-  // turned back into FP64 before its reconstruction, and the trailing update
-  // writes the finished R rows as FP64.
+  bool oz;
+  CANDMC_RET(check_form(precision, b, &oz));
+  // emulated and fp32 forms: the not-yet-factored part lives as df64 pairs;
+  // each panel is turned back into FP64 before its reconstruction, and the
+  // trailing update writes the finished R rows as FP64.
   if (oz) CANDMC_RET(to_df64(A, lda, m, k, s));
   int64_t r0 = 0;
   for (;;) {
@@ -328,11 +340,7 @@ static int qr_2d_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, do
       CANDMC_RET(materialize(mref(P, lda, 0, kUnitLower), mm, bb, aggreg_Y + r0 * lda_aY + r0,
                              lda_aY, s));
     if (kk - b > 0 && mm - b > 0) {
-      if (oz)
-        CANDMC_RET(apply_qt_ozaki(P, lda, kUnitLower, mm, (int)b, mref(tb.d(), b, 1, kUpper),
-                                  P + b * lda, lda, kk - b, b, st, s));
-      else
-        CANDMC_RET(apply_qt(P, lda, mm, (int)b, tb.d(), b, P + b * lda, lda, kk - b, precision, s));
+      CANDMC_RET(update_cols(P, lda, mm, b, tb.d(), b, kk - b, st, precision, s));
       r0 += b;
     } else {
       break;
@@ -577,7 +585,7 @@ int candmc_QR_2D_host(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, i
     CANDMC_RET(st.init(s));
     CANDMC_RET(dA.in(A, lda, m, k, s));
     // the lookahead pipeline: the same factorization as qr_2d_dev, panels overlapped
-    CANDMC_RET(qr_2d_pipe_dev(dA.d.d(), dA.ldd, m, k, b, st.p(), precision, s));
+    CANDMC_RET(qr_2d_pipe_dev(dA.d.d(), dA.ldd, m, k, b, st.p(), precision, s, nullptr));
     CANDMC_RET(dA.out(A, lda, m, k, s));
     rc = st.check(s);
   }
@@ -621,7 +629,7 @@ int candmc_QR_2D_pipe(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, i
   cudaStream_t s = STREAM(stream);
   Status st;
   CANDMC_RET(st.init(s));
-  return qr_2d_pipe_dev(A, lda, m, k, b, st.p(), precision, s);
+  return qr_2d_pipe_dev(A, lda, m, k, b, st.p(), precision, s, nullptr);
 }
 
 }  // extern "C"

@@ -54,8 +54,15 @@ int larft_from_gram(const double* G, int64_t ldg, const double* tau, int b, doub
 int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
                    double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
                    cudaStream_t s);
+// gemm_f32.cu: the same update with FP32 contractions (df64 storage of C).
+int apply_qt_f32(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top, double* C,
+                 int64_t ldc, int64_t n, int64_t fp64_rows, cudaStream_t s);
 int to_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
 int from_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
+
+// capi.cu: lookahead CAQR; Tall (nullable) receives every panel's T (b x b, ld b, panel i at i b^2).
+int qr_2d_pipe_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int* st, int precision,
+                   cudaStream_t s, double* Tall);
 
 // trailing update C <- (I - Y T Y^T)^T C in the requested arithmetic
 // (Y: unit-lower-trapezoidal m x nb read from a Y\R buffer; T upper nb x nb).

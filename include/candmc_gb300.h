@@ -178,6 +178,19 @@ int candmc_QR_2D_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int
 int candmc_QR_2D_pipe(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int precision,
                       void* stream);
 
+/* ---- least squares (no counterpart in the reference, which stops at the
+ * factorization; built from QR_2D_pipe and update_A) ---------------------------
+ * min ||A X - B||_F for A m x n (m >= n, full column rank), B m x nrhs, device
+ * pointers.  A is factored in the requested form (a copy; A itself stays
+ * resident for the residuals), X0 = R^-1 (Q^T B)[0:n] with Q applied in FP64,
+ * then up to max_refine FP64 refinement steps by corrected semi-normal
+ * equations (r = B - A X, X += R^-1 R^-T A^T r) until the largest per-column
+ * max|dX| / max|X| is <= tol.  stats (nullable, 4 doubles): steps taken, last
+ * and first relative correction, device status. */
+int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t n, const double* B, int64_t ldb,
+                    int64_t nrhs, double* X, int64_t ldx, int64_t b, int precision, int max_refine,
+                    double tol, double* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

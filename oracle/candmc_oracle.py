@@ -300,6 +300,27 @@ def QR_2D(A, b):
     return Ws
 
 
+def ls_solve(A, B, b):
+    """Least-squares oracle: QR_2D on the augmented [A | B] (the right-hand
+    sides receive Q^T B through the reference's own update_A), then
+    X = R^-1 (Q^T B)[0:n] by back substitution (dtrsm)."""
+    m, n = A.shape
+    Aug = np.hstack([np.asarray(A, dtype=np.float64), np.asarray(B, dtype=np.float64)])
+    # factor only the first n columns: panels never start inside B
+    r0 = 0
+    while r0 < n:
+        bb = min(b, n - r0)
+        YR, W = hh_recon_qr(Aug[r0:, r0:r0 + bb], bb)
+        Aug[r0:, r0:r0 + bb] = YR
+        if Aug.shape[1] - (r0 + bb) > 0 and m - r0 - bb > 0:
+            update_A(Aug[r0:, r0:r0 + bb], Aug[r0:, r0 + bb:], bb, W)
+        r0 += bb
+    R = np.triu(Aug[:n, :n])
+    X = np.array(Aug[:n, n:])
+    lp.dtrsm('L', 'U', 'N', 'N', 1.0, R, X)
+    return X
+
+
 def tau_recon_lower(Y, b, lapack_zero=False):
     """tau_i = 2/(1 + ||Y[i+1:, i]||^2) (alg/shared/util.cxx:437-466, 'L').
 

@@ -126,6 +126,16 @@ def test_QR_2D_reference_criterion_rank_deficient_fixture(m, k, b):
     assert co.backward_error(A0, A) <= 1e-13
 
 
+@pytest.mark.parametrize("m,n,b", [(600, 200, 64), (300, 300, 32), (1000, 130, 128)])
+def test_ls_oracle_matches_lapack_lstsq(m, n, b):
+    """The least-squares oracle (QR_2D on [A | B] + back substitution) against LAPACK's gelsd."""
+    A = fx.gaussian(m, n, m + n)
+    B = fx.gaussian(m, 3, 2)
+    X = co.ls_solve(A, B, b)
+    Xl = np.linalg.lstsq(A, B, rcond=None)[0]
+    assert np.abs(X - Xl).max() <= 1e-12 * max(1.0, np.abs(Xl).max())
+
+
 def test_invT_identities(golden):
     name, m, b = "hh_384x64", 384, 64
     YR, W, T = golden[name + "/YR"], golden[name + "/W"], golden[name + "/T"]
