@@ -246,6 +246,30 @@ def ls_solve(A, B, b=128, precision="fp64", max_refine=20, tol=1e-15, stream=Non
                "status": int(st[3])}
 
 
+def set_tuning(key, value):
+    """Set a tuning knob of the library ("leaf_rows": target rows per TSQR leaf)."""
+    check(lib().candmc_set_tuning(key.encode(), int(value)), "set_tuning")
+
+
+def batched_ls(As, Bs, nstreams=16, use_graph=False, stream=None):
+    """Solve min ||A_i x_i - b_i|| for lists of column-major CUDA tensors A_i (m_i x n_i,
+    n_i <= 128) and b_i (m_i x 1).  A_i becomes Y\\R, b_i becomes Q^T b_i with
+    x_i = b_i[:n_i].  Returns the list of x_i views."""
+    import ctypes
+    k = len(As)
+    arr = lambda t, vals: (t * k)(*vals)
+    ms = [a.shape[0] for a in As]
+    ns = [a.shape[1] for a in As]
+    pa = [_dev(a, "A")[0] for a in As]
+    la = [_dev(a, "A")[1] for a in As]
+    pb = [_dev(b, "B")[0] for b in Bs]
+    check(lib().candmc_batched_ls(k, arr(ctypes.c_int64, ms), arr(ctypes.c_int64, ns),
+                                  arr(ctypes.c_void_p, pa), arr(ctypes.c_int64, la),
+                                  arr(ctypes.c_void_p, pb), int(nstreams), int(bool(use_graph)),
+                                  _stream(stream)), "batched_ls")
+    return [b[:n] for b, n in zip(Bs, ns)]
+
+
 def QR_2D_2D(A, b, b_sub, aggreg_Y=None, precision="fp64", stream=None):
     """Two-level blocked CAQR (alg/QR/qr_2d/qr_2d.h:176-188)."""
     m, k = A.shape

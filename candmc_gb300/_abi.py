@@ -38,6 +38,8 @@ SIGNATURES = {
     "candmc_QR_2D_pipe": [_vp, _i64, _i64, _i64, _i64, _int, _vp],
     "candmc_ls_solve": [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int, _int,
                         ctypes.c_double, _vp, _vp],
+    "candmc_batched_ls": [_i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp],
+    "candmc_set_tuning": [ctypes.c_char_p, _i64],
     "candmc_launch_count": [],
     "candmc_profile_begin": [ctypes.c_uint],
     "candmc_profile_end": [_int, _vp, _vp, _vp],

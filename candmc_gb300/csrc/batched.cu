@@ -1,0 +1,187 @@
+// Batched least squares of many independent, unevenly sized tall-skinny
+// problems: min ||A_i x_i - b_i|| with n_i <= 128 (one panel each).
+//
+// The reference solves one panel at a time (hh_recon_qr,
+// alg/QR/hh_recon/hh_recon.cxx:129-321); a batch of uneven problems on one GPU
+// needs concurrency instead: problems are sorted by cost (m_i n_i^2) and dealt
+// round-robin onto a pool of streams, so the small ones fill the SMs that the
+// large ones' TSQR trees leave idle.  Per problem: TSQR-HR of A_i (A_i becomes
+// Y\R), Q^T b_i in FP64 with the panel's T, and back substitution with R by
+// one warp (b_i's first n_i entries become x_i, as LAPACK's dgels returns it).
+// With use_graph the whole fork/join schedule is captured once into a CUDA
+// graph (keyed by the sizes, pointers and tuning) and replayed afterwards.
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace candmc {
+
+// R x = c in place on x (R upper, n x n, ld ldr), one warp.
+__global__ void k_trsv_upper(const double* R, int64_t ldr, int n, double* x) {
+  const int lane = threadIdx.x;
+  for (int i = n - 1; i >= 0; --i) {
+    double s = 0.0;
+    for (int j = i + 1 + lane; j < n; j += 32) s = fma(R[(int64_t)j * ldr + i], x[j], s);
+    s = warp_sum(s);
+    if (lane == 0) x[i] = (x[i] - s) / R[(int64_t)i * ldr + i];
+    __syncwarp();
+  }
+}
+
+struct StreamPool {
+  std::vector<cudaStream_t> s;
+  cudaStream_t get(int i) {
+    while ((int)s.size() <= i) {
+      cudaStream_t t = nullptr;
+      if (cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+      s.push_back(t);
+    }
+    return s[i];
+  }
+};
+
+static StreamPool g_pool[64];
+static std::mutex g_graph_mu;
+static std::map<std::vector<int64_t>, cudaGraphExec_t> g_graphs;
+
+static int batched_issue(int64_t nprob, const int64_t* m, const int64_t* n, double* const* A,
+                         const int64_t* lda, double* const* B, int nstreams, cudaStream_t s) {
+  int dev = 0;
+  CANDMC_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(CANDMC_ERR_ARG, "device index");
+  std::vector<int64_t> order(nprob);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+    return (double)m[a] * n[a] * n[a] > (double)m[b] * n[b] * n[b];
+  });
+  int64_t tsz = 0;
+  std::vector<int64_t> toff(nprob);
+  for (int64_t i = 0; i < nprob; ++i) {
+    toff[i] = tsz;
+    tsz += n[i] * n[i];
+  }
+  DevBuf tbuf, stw;
+  CANDMC_RET(tbuf.alloc(sizeof(double) * std::max<int64_t>(tsz, 1), s));
+  CANDMC_RET(stw.alloc(sizeof(int), s));
+  CANDMC_CK(cudaMemsetAsync(stw.p, 0, sizeof(int), s));
+  cudaEvent_t fork;
+  CANDMC_CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  CANDMC_CK(cudaEventRecord(fork, s));
+  std::vector<cudaEvent_t> joins;
+  const int ns = std::max(1, std::min<int>(nstreams, (int)nprob));
+  int rc = CANDMC_OK;
+  for (int k = 0; k < ns && rc == CANDMC_OK; ++k) {
+    cudaStream_t sk = g_pool[dev].get(k);
+    if (!sk) { rc = set_error(CANDMC_ERR_CUDA, "stream pool"); break; }
+    if (cudaStreamWaitEvent(sk, fork, 0) != cudaSuccess) { rc = CANDMC_ERR_CUDA; break; }
+    for (int64_t q = k; q < nprob; q += ns) {
+      const int64_t i = order[q];
+      double* T = tbuf.d() + toff[i];
+      rc = hr_rec(A[i], lda[i], m[i], (int)n[i], T, n[i], static_cast<int*>(stw.p), CANDMC_PREC_FP64, sk);
+      if (rc != CANDMC_OK) break;
+      rc = apply_qt(A[i], lda[i], m[i], (int)n[i], T, n[i], B[i], m[i], 1, CANDMC_PREC_FP64, sk);
+      if (rc != CANDMC_OK) break;
+      {
+        ProfScope ps(CANDMC_KCLASS_SMALL, (double)n[i] * n[i], sk);
+        k_trsv_upper<<<1, 32, 0, sk>>>(A[i], lda[i], (int)n[i], B[i]);
+      }
+      if (cudaGetLastError() != cudaSuccess) { rc = CANDMC_ERR_CUDA; break; }
+    }
+    cudaEvent_t j;
+    if (cudaEventCreateWithFlags(&j, cudaEventDisableTiming) != cudaSuccess) { rc = CANDMC_ERR_CUDA; break; }
+    joins.push_back(j);
+    if (cudaEventRecord(j, sk) != cudaSuccess) rc = CANDMC_ERR_CUDA;
+  }
+  for (auto j : joins) {
+    cudaStreamWaitEvent(s, j, 0);
+    cudaEventDestroy(j);
+  }
+  cudaEventDestroy(fork);
+  return rc;
+}
+
+}  // namespace candmc
+
+using namespace candmc;
+
+extern "C" int candmc_set_tuning(const char* key, int64_t value) {
+  if (!key) return set_error(CANDMC_ERR_ARG, "tuning key");
+  if (std::string(key) == "leaf_rows") {
+    if (value < 32 || value > 256) return set_error(CANDMC_ERR_ARG, "leaf_rows in [32, 256]");
+    g_leaf_rows = value;
+    return CANDMC_OK;
+  }
+  return set_error(CANDMC_ERR_ARG, "unknown tuning key");
+}
+
+extern "C" int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t* n, double* const* A,
+                                 const int64_t* lda, double* const* B, int nstreams, int use_graph,
+                                 void* stream) {
+  if (nprob < 0 || (nprob > 0 && (!m || !n || !A || !lda || !B)))
+    return set_error(CANDMC_ERR_ARG, "batched_ls args");
+  for (int64_t i = 0; i < nprob; ++i)
+    if (n[i] < 1 || n[i] > 128 || m[i] < n[i] || lda[i] < m[i] || !A[i] || !B[i])
+      return set_error(CANDMC_ERR_ARG, "batched_ls: each problem needs 1 <= n <= 128 and m >= n");
+  if (nprob == 0) return CANDMC_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!use_graph) return batched_issue(nprob, m, n, A, lda, B, nstreams, s);
+  std::vector<int64_t> key;
+  key.reserve(6 * nprob + 3);
+  key.push_back(nprob);
+  key.push_back(nstreams);
+  key.push_back(g_leaf_rows);
+  for (int64_t i = 0; i < nprob; ++i) {
+    key.push_back(m[i]);
+    key.push_back(n[i]);
+    key.push_back(lda[i]);
+    key.push_back((int64_t)(uintptr_t)A[i]);
+    key.push_back((int64_t)(uintptr_t)B[i]);
+  }
+  // the schedule is captured on (and replayed from) a stream of the library's
+  // own, joined to the caller's stream by events, so the caller's stream may be
+  // the legacy default stream (which cannot be captured)
+  int dev = 0;
+  CANDMC_CK(cudaGetDevice(&dev));
+  cudaStream_t cs = g_pool[dev].get(63);
+  if (!cs) return set_error(CANDMC_ERR_CUDA, "capture stream");
+  cudaGraphExec_t exec = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_graph_mu);
+    auto it = g_graphs.find(key);
+    if (it != g_graphs.end()) exec = it->second;
+  }
+  if (!exec) {
+    // kernel attributes are set by an eager run first (not a stream operation)
+    cudaGraph_t graph = nullptr;
+    CANDMC_CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    int rc = batched_issue(nprob, m, n, A, lda, B, nstreams, cs);
+    cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    if (rc != CANDMC_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CANDMC_CK(e);
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CANDMC_CK(e);
+    std::lock_guard<std::mutex> g(g_graph_mu);
+    g_graphs[key] = exec;
+  }
+  cudaEvent_t e0, e1;
+  CANDMC_CK(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
+  CANDMC_CK(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(e0, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, e0, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, cs);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, cs);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, e1, 0);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CANDMC_CK(e);
+  return CANDMC_OK;
+}

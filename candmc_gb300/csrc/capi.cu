@@ -88,7 +88,7 @@ int apply_qt(const double* Y, int64_t ldy, int64_t m, int nb, const double* T, i
 
 // Recursive blocked TSQR-HR (see file comment).  T (ldT) receives the b x b
 // upper-triangular factor; the strictly lower part of T is zeroed.
-static int hr_rec(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, int* st,
+int hr_rec(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, int* st,
                   int precision, cudaStream_t s) {
   if (b <= kDirectB) return hr_direct4(A, lda, m, b, T, ldT, nullptr, 0, st, s);
   const int b1 = b / 2, b2 = b - b1;

@@ -26,6 +26,7 @@ class ProfScope {
 int hr_direct(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
               int64_t ldW, int* d_status, cudaStream_t s);
 // tsqr4.cu: direct TSQR-HR with a fan-in-4 tree and compact-WY Q blocks.
+extern int64_t g_leaf_rows;
 int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
                int64_t ldW, int* d_status, cudaStream_t s);
 
@@ -60,6 +61,9 @@ int apply_qt_f32(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, Mat
 int to_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
 int from_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
 
+// capi.cu: TSQR-HR of one m x b panel (recursive blocking), T (ldT) out.
+int hr_rec(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, int* st, int precision,
+           cudaStream_t s);
 // capi.cu: lookahead CAQR; Tall (nullable) receives every panel's T (b x b, ld b, panel i at i b^2).
 int qr_2d_pipe_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int* st, int precision,
                    cudaStream_t s, double* Tall);

@@ -33,6 +33,9 @@
 namespace candmc {
 
 constexpr int kFan = 4;
+
+// Target rows per TSQR leaf (tuning knob, candmc_set_tuning("leaf_rows", v)).
+int64_t g_leaf_rows = 64;
 constexpr int kTriScratch = 512 + kDirectB * kDirectB;   // h4_tri_inv workspace (doubles)
 
 __device__ __forceinline__ int64_t t4_leaf_row0(int64_t m, int P, int i) {
@@ -552,7 +555,8 @@ __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
 int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
                int64_t ldW, int* d_status, cudaStream_t s) {
   if (b < 1 || b > kDirectB || m < b) return CANDMC_ERR_ARG;
-  int64_t P = std::max<int64_t>(1, std::min<int64_t>(m / 64, m / b));
+  const int64_t leaf_rows = std::max<int64_t>(32, std::min<int64_t>(g_leaf_rows, 256));
+  int64_t P = std::max<int64_t>(1, std::min<int64_t>(m / leaf_rows, m / b));
   if (P > (1 << 24)) return CANDMC_ERR_ARG;
   Hr4Args a{};
   a.P = (int)P;

@@ -191,6 +191,20 @@ int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t n, const do
                     int64_t nrhs, double* X, int64_t ldx, int64_t b, int precision, int max_refine,
                     double tol, double* stats, void* stream);
 
+/* ---- batched least squares (no counterpart in the reference) ----------------
+ * nprob independent problems min ||A_i x_i - b_i|| with 1 <= n_i <= 128 and
+ * m_i >= n_i; host arrays of sizes and DEVICE pointers.  A_i (ld lda[i])
+ * becomes Y\R of its TSQR-HR; b_i (m_i x 1) becomes Q^T b_i with x_i in its
+ * first n_i entries (the dgels convention).  Problems are sorted by cost and
+ * dealt onto nstreams streams; use_graph != 0 captures the schedule into a
+ * CUDA graph on first use (keyed by sizes, pointers, nstreams and tuning) and
+ * replays it afterwards. */
+int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t* n, double* const* A,
+                      const int64_t* lda, double* const* B, int nstreams, int use_graph, void* stream);
+
+/* tuning knobs: "leaf_rows" (target rows per TSQR leaf, 32..256, default 64) */
+int candmc_set_tuning(const char* key, int64_t value);
+
 #ifdef __cplusplus
 }
 #endif

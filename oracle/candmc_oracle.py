@@ -312,8 +312,9 @@ def ls_solve(A, B, b):
         bb = min(b, n - r0)
         YR, W = hh_recon_qr(Aug[r0:, r0:r0 + bb], bb)
         Aug[r0:, r0:r0 + bb] = YR
-        if Aug.shape[1] - (r0 + bb) > 0 and m - r0 - bb > 0:
-            update_A(Aug[r0:, r0:r0 + bb], Aug[r0:, r0 + bb:], bb, W)
+        # every panel's Q^T reaches B, including a square last panel (whose
+        # reconstructed last reflector is a sign flip, not the identity)
+        update_A(Aug[r0:, r0:r0 + bb], Aug[r0:, r0 + bb:], bb, W)
         r0 += bb
     R = np.triu(Aug[:n, :n])
     X = np.array(Aug[:n, n:])

@@ -46,6 +46,20 @@ def haar(n, rng, ncols=None):
     return Q * np.sign(np.diag(R))[None, :]
 
 
+def batched_problems(count, seed=3, m_lo=256, m_hi=262144, widths=(8, 16, 32, 64, 128)):
+    """Uneven least-squares problem set: per-problem PCG64 streams from
+    SeedSequence(seed).spawn(count); m_i = round(exp(U(ln m_lo, ln m_hi))),
+    n_i uniform over `widths` (m_i >= n_i enforced), A_i and b_i ~ N(0, 1).
+    Returns a list of (m, n, generator) so callers can draw A_i, b_i lazily."""
+    out = []
+    for ss in np.random.SeedSequence(seed).spawn(count):
+        rng = np.random.default_rng(ss)
+        m = int(round(np.exp(rng.uniform(np.log(m_lo), np.log(m_hi)))))
+        n = int(rng.choice(widths))
+        out.append((max(m, n), n, rng))
+    return out
+
+
 def svd_matrix(m, n, seed, sigma_min):
     """A = U diag(sigma) V^T, U (m x n) and V (n x n) Haar from PCG64(seed), U drawn first,
     sigma log-spaced from 1 to sigma_min."""
