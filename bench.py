@@ -1,26 +1,39 @@
 #!/usr/bin/env python
-"""CAQR benchmark on GB300: the reference's 2D QR (QR_2D) of one square matrix.
+"""Benchmarks of the CANDMC QR hot path on GB300.
 
-Workload (the configuration the headline metric is quoted on): n = 16384,
-float64, A = U diag(sigma) V^T with U, V Haar-orthogonal (Mezzadri's
-Q*diag(sign(diag R)) of Gaussian draws from numpy PCG64(seed=1), U drawn
-first), sigma log-spaced from 1 to 1e-6, panel width b = 128: every panel is
-factored by TSQR + Householder reconstruction and the trailing matrix is
-updated with A -= Y T^T (Y^T A).
+Default workload (the configuration the headline metric is quoted on):
+`caqr` -- the reference's 2D QR of one square matrix, n = 16384, float64,
+A = U diag(sigma) V^T with U, V Haar-orthogonal (Mezzadri's Q*diag(sign(diag
+R)) of Gaussian draws from numpy PCG64(seed=1), U drawn first), sigma
+log-spaced from 1 to 1e-6, panel width b = 128: every panel is factored by
+TSQR + Householder reconstruction and the trailing matrix is updated with
+A -= Y T^T (Y^T A).  One step = restore A from the device-resident input
+(2 GiB D2D copy) + one full factorization; the 2 GiB input is larger than L2
+(129 MB), so no flush is needed between steps.  Metric: FP64-equivalent
+TFLOP/s = (4/3 n^3) / step time (the reference's GFlops formula
+2mk^2 - 2/3 k^3 at m = k, bench/QR/bench_qr_2d.cxx:85-87).
 
-One step = restore A from the device-resident input (2 GiB D2D copy) + one
-full factorization.  The 2 GiB input is larger than L2 (129 MB), so no flush
-is needed between steps.  Metric: FP64-equivalent TFLOP/s = (4/3 n^3) / step
-time (the reference's own GFlops formula 2mk^2 - 2/3 k^3 at m = k,
-bench/QR/bench_qr_2d.cxx:85-87).
+Other workloads (`--workload`), one JSON line each in the same format:
+  tsqr_hr  TSQR-HR of one 8192 x 64 N(0,1) panel (seed 0): hh_recon_qr,
+           L2 flushed between steps.
+  forms    precision forms of CAQR at m = 32768, n = 16384 (U, V Haar from
+           seed 2, sigma to 1e-10 and to 1e-3): QR_2D_pipe in the ozaki, fp32
+           and fp64 forms, then least squares with 16 N(0,1) right-hand sides
+           refined in FP64.
+  batched  4096 uneven least-squares problems in one batched call (m
+           log-uniform in [256, 262144], n in {8,16,32,64,128}), autotuned,
+           CUDA-graph replay; metric solves/s.
+  serve    the least-squares request server under Poisson arrivals (seed 4)
+           at 1k..50k requests/s, m log-uniform in [512, 1048576], n in
+           {16,32,64,128,256}; FP32 CAQR + FP64 refinement; p50/p99 latency
+           and solves/s beside the plain FP64 one-request-at-a-time path.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl candmc|reference]
+    python bench.py [--workload W] [--gpus N] [--steps K] [--warmup W] [--impl candmc|reference]
 
-N > 1 (torchrun) runs N independent replicas (the factorization of one
-matrix is not sharded across GPUs here), value = N * flops / max time.
-`--impl reference` times the reference's own single-rank call sequence
-(dgeqrf, dorgqr, signed LU, dtrsm, dgemm: oracle/reference_lapack.py) on the
-host cores with all BLAS threads, on a bounded n = 8192 sample.
+N > 1 (torchrun) runs N independent replicas (the problems are not sharded
+across GPUs), value = N * work / max time.  `--impl reference` times the
+reference's own single-rank call sequence (dgeqrf, dorgqr, signed LU, dtrsm,
+dgemm: oracle/reference_lapack.py) on the host cores on a bounded sample.
 """
 import argparse
 import json
@@ -37,24 +50,35 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FP64_PEAK_GF = 1170.0   # measured DFMA rate of this GB300 (chip-wide microbenchmark)
+WORKLOADS = ("caqr", "tsqr_hr", "forms", "batched", "serve")
 
 
 def parse():
     p = argparse.ArgumentParser()
+    p.add_argument("--workload", choices=WORKLOADS, default="caqr")
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["candmc", "reference"], default="candmc")
-    p.add_argument("--n", type=int, default=16384)
-    p.add_argument("--b", type=int, default=128)
-    p.add_argument("--form", choices=["fp64", "ozaki"], default="ozaki")
+    p.add_argument("--m", type=int, default=None)
+    p.add_argument("--n", type=int, default=None)
+    p.add_argument("--b", type=int, default=None)
+    p.add_argument("--form", choices=["fp64", "ozaki", "fp32"], default=None)
+    p.add_argument("--forms", default="ozaki,fp32,fp64")
     p.add_argument("--entry", choices=["pipe", "qr2d"], default="pipe",
                    help="QR_2D_pipe (lookahead, the reference tests' default) or QR_2D")
     p.add_argument("--sigma-min", type=float, default=1e-6)
-    p.add_argument("--seed", type=int, default=1)
-    p.add_argument("--ref-n", type=int, default=8192, help="bounded CPU sample size")
+    p.add_argument("--seed", type=int, default=None)
+    p.add_argument("--ref-n", type=int, default=8192, help="bounded CPU sample size (caqr)")
+    p.add_argument("--count", type=int, default=None, help="problems (batched) / requests per rate (serve)")
+    p.add_argument("--rates", default="1000,2000,5000,10000,20000,50000")
+    p.add_argument("--workers", type=int, default=12)
+    p.add_argument("--budget-gb", type=float, default=120.0)
+    p.add_argument("--no-graph", action="store_true")
+    p.add_argument("--no-tune", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
     return p.parse_args()
 
 
@@ -62,31 +86,47 @@ def flops(n):
     return 4.0 / 3.0 * float(n) ** 3
 
 
+def qr_flops(m, n):
+    return 2.0 * m * n * n - 2.0 / 3.0 * float(n) ** 3
+
+
 # ----------------------------------------------------------------- inputs
-def make_input_gpu(n, seed, sigma_min, device):
-    """A = U diag(sigma) V^T, U and V Haar from PCG64(seed) (U first), on the GPU."""
+def _preload_linalg():
+    """torch loads its CUDA linear-algebra library lazily by bare name; load it
+    by path first so the lookup also succeeds under a profiler's injection."""
     import ctypes
 
     import torch
-    # torch loads its CUDA linear-algebra library lazily by bare name; load it
-    # by path first so the lookup also succeeds under a profiler's injection.
     linalg = os.path.join(os.path.dirname(torch.__file__), "lib", "libtorch_cuda_linalg.so")
     if os.path.exists(linalg):
         ctypes.CDLL(linalg, mode=ctypes.RTLD_GLOBAL)
+
+
+def haar_gpu(rng, rows, cols, device):
+    """Haar-distributed orthonormal columns (rows x cols): Q diag(sign(diag R))
+    of a Gaussian matrix drawn from rng (row-major draws), QR on the GPU."""
+    import torch
+    G = torch.from_numpy(rng.standard_normal((rows, cols))).to(device)
+    Q, R = torch.linalg.qr(G)
+    Q *= torch.sign(torch.diagonal(R))[None, :]
+    del G, R
+    return Q
+
+
+def make_input_gpu(n, seed, sigma_min, device, m=None):
+    """A = U diag(sigma) V^T (m x n, default square), U and V Haar from
+    PCG64(seed) (U first), sigma log-spaced from 1 to sigma_min; column-major."""
+    import torch
+    _preload_linalg()
+    m = m or n
     rng = np.random.default_rng(seed)
-    mats = []
-    for _ in range(2):
-        G = torch.from_numpy(rng.standard_normal((n, n))).to(device)
-        Q, R = torch.linalg.qr(G)
-        Q *= torch.sign(torch.diagonal(R))[None, :]
-        mats.append(Q)
-        del G, R
-    U, V = mats
+    U = haar_gpu(rng, m, n, device)
+    V = haar_gpu(rng, n, n, device)
     s = torch.logspace(0, np.log10(sigma_min), n, dtype=torch.float64, device=device)
     A = (U * s[None, :]) @ V.t()
     del U, V
     torch.cuda.synchronize()
-    return A.t().contiguous().t()   # column-major
+    return A.t().contiguous().t(), rng
 
 
 # ----------------------------------------------------------------- clocks
@@ -157,6 +197,11 @@ def traffic_from_profile(name):
     return float(m.group(1)) if m else None
 
 
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(path)) if os.path.exists(path) else {}
+
+
 def sampled_backward_error(cm, A0, YR, b, ncols=64, seed=0):
     """||Q^T A0[:, S] - R[:, S]||_F / ||A0[:, S]||_F over a random column sample S.
 
@@ -164,63 +209,162 @@ def sampled_backward_error(cm, A0, YR, b, ncols=64, seed=0):
     the reference tests' residual restricted to sampled columns.
     """
     import torch
-    n = A0.shape[0]
+    m, n = YR.shape
     rng = np.random.default_rng(seed)
     S = torch.from_numpy(np.sort(rng.choice(n, size=min(ncols, n), replace=False))).to(A0.device)
     X = A0[:, S].t().contiguous().t()
     for r0 in range(0, n, b):
         bb = min(b, n - r0)
-        if n - r0 <= 0:
-            break
         cm.update_A(YR[r0:, r0:r0 + bb], X[r0:, :], bb, None)
     R = torch.triu(YR)[:, S]
     torch.cuda.synchronize()
     return float(torch.linalg.norm(X - R) / torch.linalg.norm(A0[:, S]))
 
 
-# ----------------------------------------------------------------- reference arm
-def run_reference(args, world, rank):
-    if rank != 0:
-        return 0
-    from oracle import fixtures as fx
-    from oracle import reference_lapack as rl
-    n = args.ref_n
-    rng = np.random.default_rng(args.seed)
-    A0 = np.asfortranarray(fx.svd_matrix(n, n, args.seed, args.sigma_min)) if n <= 4096 else \
-        np.asfortranarray(rng.standard_normal((n, n)))
-    times = []
-    for it in range(args.warmup + args.steps):
-        A = A0.copy(order="F")
-        t0 = time.perf_counter()
-        rl.QR_2D_lapack(A, args.b)
-        dt = time.perf_counter() - t0
-        if it >= args.warmup:
-            times.append(dt)
-    tot = sum(times)
-    val = flops(n) * len(times) / tot / 1e12
-    cores = rl.blas_threads()
-    line = {
-        "impl": "reference",
-        "metric": "CAQR TFLOP/s (FP64-equivalent, 4/3 n^3 per factorization)",
-        "value": val, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"CAQR QR_2D n={args.n} b={args.b} float64 (timed on a bounded "
-                               f"n={n} sample on the host cores)",
-                   "n": args.n, "b": args.b, "sample_n": n, "form": "reference LAPACK call sequence",
-                   "parallelism": "host BLAS threads"},
-        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-                         "sample": f"QR_2D_lapack n={n} (bounded sample of the n={args.n} workload; "
-                                   "Gaussian input above n=4096)"},
-        "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
-    return 0
+class Ctx:
+    """What every workload needs: the library, the device, the process group."""
+
+    def __init__(self, args):
+        import torch
+        self.args = args
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(self.local)
+        self.dev = torch.device("cuda", self.local)
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl", device_id=self.dev)
+            self.dist = dist
+        from candmc_gb300 import build as _build
+        _build.build()
+        import candmc_gb300 as cm
+        from candmc_gb300 import _abi
+        self.cm, self.abi, self.lib = cm, _abi, cm.lib()
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max_over_ranks(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([x], device=self.dev, dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(self, step, steps, classes=(), flush=None):
+        """Run `steps` steps inside the timed region: barrier + synchronize on
+        both sides, CUDA events on the launching (current) stream, clocks
+        sampled throughout, kernel classes timed live.  With `flush`, the L2
+        flush runs before each step outside the per-step event pair."""
+        import ctypes
+
+        import torch
+        mask = 0
+        for c in classes:
+            mask |= 1 << self.abi.KCLASS[c]
+        self.barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(gpu_id_for_smi(self.local))
+        l0 = self.lib.candmc_launch_count()
+        self.lib.candmc_profile_begin(mask)
+        if flush is None:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(steps):
+                step()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+        else:
+            pairs = []
+            for _ in range(steps):
+                flush()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                step()
+                e1.record()
+                pairs.append((e0, e1))
+            torch.cuda.synchronize()
+            ms = sum(a.elapsed_time(b) for a, b in pairs)
+        self.barrier()
+        launches = self.lib.candmc_launch_count() - l0
+        nc = self.abi.NKCLASS
+        kms = (ctypes.c_double * nc)()
+        kwork = (ctypes.c_double * nc)()
+        kl = (ctypes.c_longlong * nc)()
+        self.lib.candmc_profile_end(nc, kms, kwork, kl)
+        clk = clocks.stop()
+        prof = {c: (kms[self.abi.KCLASS[c]], kwork[self.abi.KCLASS[c]], kl[self.abi.KCLASS[c]])
+                for c in classes}
+        return self.max_over_ranks(ms), launches, prof, clk
 
 
-def cpu_baseline(args):
+def fp64_roof(prof, classes, kernel, step_ms):
+    ms = sum(prof[c][0] for c in classes)
+    work = sum(prof[c][1] for c in classes)
+    launches = sum(prof[c][2] for c in classes)
+    achieved = work / (ms / 1e3) / 1e12 if ms > 0 else None
+    return {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_GF / 1e3, "unit": "TFLOP/s",
+            "frac": achieved / (FP64_PEAK_GF / 1e3) if achieved else None, "traffic": None,
+            "kernel": kernel, "launches": launches, "share_of_step": ms / step_ms if step_ms else None,
+            "peak_source": "DFMA microbenchmark on this GB300 (FP64 is not in MEASURED_PEAKS.json); "
+                           "FP64 is neither the HBM nor the tensor roof"}
+
+
+def base_line(args, ctx, metric, value, unit, ms_per_step, dtype, config, higher=True):
+    return {"metric": metric, "value": value, "unit": unit, "n_gpus": ctx.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": higher,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config}
+
+
+# ----------------------------------------------------------------- CPU legs
+def _cpu_ls_task(task):
+    """One least-squares problem by the reference call sequence, single BLAS
+    thread (run inside a spawned worker); returns the solve's seconds."""
+    m, n, seed = task
     from oracle import reference_lapack as rl
-    n = min(args.ref_n, args.n)
+    rng = np.random.default_rng(seed)
+    A = np.asfortranarray(rng.standard_normal((m, n)))
+    b = rng.standard_normal((m, 1))
+    t0 = time.perf_counter()
+    rl.ls_solve_lapack(A, b, 128)
+    return time.perf_counter() - t0
+
+
+def cpu_ls_rate(tasks, seconds):
+    """Solves/s of the reference call sequence over `tasks` (m, n, seed), one
+    single-threaded process per host core, stopping after ~`seconds` of
+    solve time per core; generation is excluded from the timed solves."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    old = os.environ.get("OPENBLAS_NUM_THREADS")
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    try:
+        with mp.get_context("spawn").Pool(cores) as pool:
+            done, total = 0, 0.0
+            it = pool.imap(_cpu_ls_task, tasks, chunksize=1)
+            for dt in it:
+                done += 1
+                total += dt
+                if total / cores >= seconds:
+                    pool.terminate()
+                    break
+    finally:
+        if old is None:
+            os.environ.pop("OPENBLAS_NUM_THREADS", None)
+        else:
+            os.environ["OPENBLAS_NUM_THREADS"] = old
+    return done / (total / cores), done, cores
+
+
+def cpu_caqr(args, n):
+    from oracle import reference_lapack as rl
     rng = np.random.default_rng(args.seed)
     A0 = np.asfortranarray(rng.standard_normal((n, n)))
     rl.QR_2D_lapack(A0.copy(order="F")[: n // 4, : n // 4].copy(order="F"), args.b)  # warm-up
@@ -234,34 +378,98 @@ def cpu_baseline(args):
                       f"b={args.b}, Gaussian input, one factorization ({dt:.1f} s)"}
 
 
-# ----------------------------------------------------------------- main
-def main():
-    args = parse()
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+def cpu_tsqr_hr(args, m, b, reps=None):
+    from oracle import reference_lapack as rl
+    A0 = np.asfortranarray(np.random.default_rng(0).standard_normal((m, b)))
+    Af = A0.copy(order="F").reshape(-1, order="F")
+    rl.hh_recon_qr_lapack(Af, m, 0, m, b)
+    times = []
+    t_end = time.perf_counter() + args.cpu_seconds
+    while (reps is None and time.perf_counter() < t_end) or (reps is not None and len(times) < reps):
+        Af = A0.copy(order="F").reshape(-1, order="F")
+        t0 = time.perf_counter()
+        rl.hh_recon_qr_lapack(Af, m, 0, m, b)
+        times.append(time.perf_counter() - t0)
+    return qr_flops(m, b) * len(times) / sum(times) / 1e9, len(times), rl.blas_threads()
+
+
+# ----------------------------------------------------------------- reference arm
+def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
-        return run_reference(args, world, rank)
+    if rank != 0:
+        return 0
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    wl = args.workload
+    line = {"impl": "reference", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "scaling": "weak", "vs_baseline": None, "data": "synthetic", "higher_is_better": True}
+    if wl == "caqr":
+        from oracle import fixtures as fx
+        from oracle import reference_lapack as rl
+        n = args.ref_n
+        rng = np.random.default_rng(args.seed)
+        A0 = np.asfortranarray(fx.svd_matrix(n, n, args.seed, args.sigma_min)) if n <= 4096 else \
+            np.asfortranarray(rng.standard_normal((n, n)))
+        times = []
+        for it in range(args.warmup + args.steps):
+            A = A0.copy(order="F")
+            t0 = time.perf_counter()
+            rl.QR_2D_lapack(A, args.b)
+            dt = time.perf_counter() - t0
+            if it >= args.warmup:
+                times.append(dt)
+        tot = sum(times)
+        val = flops(n) * len(times) / tot / 1e12
+        cores = rl.blas_threads()
+        line.update({
+            "metric": "CAQR TFLOP/s (FP64-equivalent, 4/3 n^3 per factorization)",
+            "value": val, "unit": "TFLOP/s", "ms_per_step": 1e3 * tot / len(times), "dtype": "f64",
+            "config": {"workload": f"CAQR QR_2D n={args.n} b={args.b} float64 (timed on a bounded "
+                                   f"n={n} sample on the host cores)",
+                       "n": args.n, "b": args.b, "sample_n": n, "form": "reference LAPACK call sequence",
+                       "parallelism": "host BLAS threads"},
+            "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                             "sample": f"QR_2D_lapack n={n} (bounded sample of the n={args.n} workload; "
+                                       "Gaussian input above n=4096)"}})
+    elif wl == "tsqr_hr":
+        gf, reps, cores = cpu_tsqr_hr(args, args.m, args.b, reps=args.warmup + args.steps)
+        line.update({"metric": "TSQR-HR GFLOP/s (2mb^2 - 2/3 b^3 per panel)", "value": gf,
+                     "unit": "GFLOP/s", "ms_per_step": qr_flops(args.m, args.b) / gf / 1e6, "dtype": "f64",
+                     "config": {"workload": f"hh_recon_qr {args.m}x{args.b} N(0,1) seed 0"},
+                     "cpu_baseline": {"value": gf, "unit": "GFLOP/s", "cores": cores, "kind": "port",
+                                      "sample": f"hh_recon_qr_lapack x{reps}"}})
+    elif wl in ("batched", "serve"):
+        if wl == "batched":
+            sizes = batched_sizes(args.count, seed=3)
+            tasks = [(m, n, 1000 + i) for i, (m, n) in enumerate(sizes)]
+            metric = "batched least squares solves/s"
+        else:
+            trace = serve_trace(args, args.count, max(float(r) for r in args.rates.split(",")))
+            tasks = [(m, n, 2000 + i) for i, (_, m, n) in enumerate(trace)]
+            metric = "least-squares requests solves/s (CPU per-request path)"
+        rate, done, cores = cpu_ls_rate(tasks, args.cpu_seconds * max(1, args.steps))
+        line.update({"metric": metric, "value": rate, "unit": "solves/s", "ms_per_step": 1e3 / rate,
+                     "dtype": "f64", "config": {"workload": wl, "sample_problems": done},
+                     "cpu_baseline": {"value": rate, "unit": "solves/s", "cores": cores, "kind": "port",
+                                      "sample": f"first {done} problems of the workload, reference call "
+                                                "sequence, one single-threaded process per core"}})
+    else:
+        print(json.dumps({"impl": "reference", "unavailable": f"no CPU reference arm for workload {wl}; "
+                          "its CPU baseline is the caqr arm"}), flush=True)
+        return 0
+    line["e2e"] = {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}
+    print(json.dumps(line), flush=True)
+    return 0
 
+
+# ----------------------------------------------------------------- caqr (default)
+def wl_caqr(args, ctx):
     import torch
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=dev)
-
-    from candmc_gb300 import build as _build
-    _build.build()
-    import candmc_gb300 as cm
-    from candmc_gb300 import _abi
-    lib = cm.lib()
-
-    n, b = args.n, args.b
-    A0 = make_input_gpu(n, args.seed + rank * 1000 if world > 1 else args.seed, args.sigma_min, dev)
+    cm, lib = ctx.cm, ctx.lib
+    n, b, prec = args.n, args.b, args.form
+    A0, _ = make_input_gpu(n, args.seed + ctx.rank * 1000 if ctx.world > 1 else args.seed,
+                           args.sigma_min, ctx.dev)
     A = torch.empty_like(A0.t()).t()
-    prec = args.form
-
     qr = cm.QR_2D_pipe if args.entry == "pipe" else cm.QR_2D
 
     def step():
@@ -271,76 +479,39 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-
-    # dominant kernel class of this form, timed live on its launching stream
-    dom = {"fp64": ["gemm_tn", "gemm_nn"], "ozaki": ["oz_tn", "oz_nn"]}[prec]
-    mask = 0
-    for c in dom:
-        mask |= 1 << _abi.KCLASS[c]
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(gpu_id_for_smi(local))
-    launches0 = lib.candmc_launch_count()
-    lib.candmc_profile_begin(mask)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        step()
-    e1.record()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    ms = e0.elapsed_time(e1)
-    launches = lib.candmc_launch_count() - launches0
-    import ctypes
-    nc = _abi.NKCLASS
-    kms = (ctypes.c_double * nc)()
-    kwork = (ctypes.c_double * nc)()
-    kl = (ctypes.c_longlong * nc)()
-    lib.candmc_profile_end(nc, kms, kwork, kl)
-    clk = clocks.stop()
-    t_max = ms
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * flops(n) * args.steps / (t_max / 1e3) / 1e12
-
-    dom_ms = sum(kms[_abi.KCLASS[c]] for c in dom)
-    dom_work = sum(kwork[_abi.KCLASS[c]] for c in dom)
-    dom_l = sum(kl[_abi.KCLASS[c]] for c in dom)
+    dom = {"fp64": ["gemm_tn", "gemm_nn"], "ozaki": ["oz_tn", "oz_nn"], "fp32": ["f32"]}[prec]
+    t_max, launches, prof, clk = ctx.timed(step, args.steps, dom)
+    value = ctx.world * flops(n) * args.steps / (t_max / 1e3) / 1e12
+    dom_ms = sum(prof[c][0] for c in dom)
+    dom_work = sum(prof[c][1] for c in dom)
+    dom_l = sum(prof[c][2] for c in dom)
     achieved = dom_work / (dom_ms / 1e3) / 1e12 if dom_ms > 0 else None
-    if prec == "fp64":
-        roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_GF / 1e3,
-                "unit": "TFLOP/s", "frac": achieved / (FP64_PEAK_GF / 1e3) if achieved else None,
-                "traffic": traffic_from_profile("gemm_f64_caqr_n16384.md"),
-                "kernel": "k_gemm_f64 (Y^T A split-K partials and A -= Y Z)",
-                "launches": dom_l, "share_of_step": dom_ms / ms if ms else None,
-                "peak_source": "DFMA microbenchmark on this GB300 (FP64 is not in MEASURED_PEAKS.json); "
-                               "FP64 is neither the HBM nor the tensor roof"}
-    else:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
-            if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    if prec == "ozaki":
         # Each FP64 product is emulated by 28 BF16 slice products (7 slices,
         # pairs i + j <= 6), so the emulated-FP64 roof is the BF16 roof / 28;
         # `achieved` counts algorithmic FP64 flops (2 m n k per contraction).
-        pk_bf16 = peaks.get("bf16_tflops_sustained", 1700.0)
+        pk_bf16 = measured_peaks().get("bf16_tflops_sustained", 1700.0)
         pk = pk_bf16 / 28.0
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s",
                 "frac": achieved / pk if achieved else None,
                 "bf16_issued_tflops": achieved * 28.0 if achieved else None,
                 "traffic": traffic_from_profile("ozaki_gemm_caqr_n16384.md"),
                 "kernel": "k_oz_mma (Ozaki BF16 slice contractions on tcgen05, Y^T A and A -= Y Z)",
-                "launches": dom_l, "share_of_step": dom_ms / ms if ms else None,
+                "launches": dom_l, "share_of_step": dom_ms / t_max if t_max else None,
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained / 28 slice products "
                                "(of measured)"}
+    elif prec == "fp32":
+        roof = {"bound": "fp32", "achieved": achieved, "peak": 73.8, "unit": "TFLOP/s",
+                "frac": achieved / 73.8 if achieved else None, "traffic": None,
+                "kernel": "k_gemm_f32 (FP32 SIMT contractions on df64 storage)", "launches": dom_l,
+                "share_of_step": dom_ms / t_max if t_max else None,
+                "peak_source": "FFMA microbenchmark on this GB300 (73.8 TFLOP/s)"}
+    else:
+        roof = fp64_roof(prof, dom, "k_gemm_f64 (Y^T A split-K partials and A -= Y Z)", t_max)
+        roof["traffic"] = traffic_from_profile("gemm_f64_caqr_n16384.md")
 
-    # accuracy of the last factorization
     bwd = sampled_backward_error(cm, A0, A, b)
 
-    # end-to-end through the host-pointer C ABI (pinned host buffers)
     e2e = None
     if not args.no_e2e:
         src = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
@@ -355,36 +526,434 @@ def main():
             dt = time.perf_counter() - t0
             if it >= 1:
                 tt += dt
-        e2e = {"value": world * flops(n) * args.steps / tt / 1e12, "unit": "TFLOP/s",
+        e2e = {"value": ctx.world * flops(n) * args.steps / tt / 1e12, "unit": "TFLOP/s",
                "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n}
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(args)
+    cpu = cpu_caqr(args, min(args.ref_n, n)) if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu \
+        else None
+    dtype = {"fp64": "f64", "ozaki": "f64 (emulated: bf16 Ozaki slices, fp32 accumulate)",
+             "fp32": "f64 panels, fp32 trailing-update contractions"}[prec]
+    line = base_line(args, ctx, "CAQR TFLOP/s (FP64-equivalent, 4/3 n^3 per factorization)", value,
+                     "TFLOP/s", t_max / args.steps, dtype,
+                     {"workload": f"CAQR QR_2D n={n} b={b} float64, A=U diag(logspace(0,"
+                                  f"{np.log10(args.sigma_min):.0f},n)) V^T, U,V Haar (PCG64 seed {args.seed})",
+                      "n": n, "b": b, "form": prec, "entry": args.entry,
+                      "parallelism": f"replicas x{ctx.world}",
+                      "l2": "input 2 GiB > L2 129 MB, no flush needed"})
+    line.update({"clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof,
+                 "cpu_baseline": cpu,
+                 "accuracy": {"backward_error_sampled": bwd, "columns": 64, "bound": 1e-13}})
+    return line
 
-    if rank == 0:
-        line = {
-            "metric": "CAQR TFLOP/s (FP64-equivalent, 4/3 n^3 per factorization)",
-            "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if prec == "fp64" else "f64 (emulated: bf16 Ozaki slices, fp32 accumulate)",
-            "data": "synthetic",
-            "config": {"workload": f"CAQR QR_2D n={n} b={b} float64, A=U diag(logspace(0,"
-                                   f"{np.log10(args.sigma_min):.0f},n)) V^T, U,V Haar (PCG64 seed {args.seed})",
-                       "n": n, "b": b, "form": prec, "parallelism": f"replicas x{world}",
-                       "l2": "input 2 GiB > L2 129 MB, no flush needed"},
-            "clocks": clk,
-            "e2e": e2e,
-            "gpu_launches": launches,
-            "roofline": roof,
-            "cpu_baseline": cpu,
-            "accuracy": {"backward_error_sampled": bwd, "columns": 64,
-                         "bound": 1e-13},
-        }
+
+# ----------------------------------------------------------------- tsqr_hr
+def wl_tsqr_hr(args, ctx):
+    import torch
+    cm = ctx.cm
+    m, b = args.m, args.b
+    A0h = np.random.default_rng(0).standard_normal((m, b))
+    A0 = cm.colmajor(torch.from_numpy(A0h).to(ctx.dev))
+    A = cm.colmajor(A0.clone())
+    W = cm.empty_colmajor(b, b, ctx.dev)
+    T = cm.empty_colmajor(b, b, ctx.dev)
+    flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device=ctx.dev)   # 512 MB > L2
+
+    def step():
+        A.copy_(A0)
+        cm.hh_recon_qr(A, W, T)
+
+    def flush():
+        flush_buf.add_(1)
+
+    for _ in range(args.warmup):
+        flush()
+        step()
+    torch.cuda.synchronize()
+    classes = ["panel_leaf", "panel_y", "small", "gemm_tn", "gemm_nn", "reduce"]
+    t_max, launches, prof, clk = ctx.timed(step, args.steps, classes, flush=flush)
+    f = qr_flops(m, b)
+    value = ctx.world * f * args.steps / (t_max / 1e3) / 1e9
+    roof = fp64_roof(prof, ["panel_leaf", "panel_y"],
+                     "k_hr4_leaf_tree + k_hr4_form_y (TSQR leaves, fan-in-4 tree, reconstruction, Y)",
+                     t_max)
+    hbm = measured_peaks().get("hbm_gbs", 6778.0)
+    bytes_alg = 16.0 * m * b
+    roof["hbm"] = {"achieved_gbs": bytes_alg * args.steps / (t_max / 1e3) / 1e9, "peak_gbs": hbm,
+                   "frac": bytes_alg * args.steps / (t_max / 1e3) / 1e9 / hbm,
+                   "note": "algorithmic bytes 16 m b (read A, write Y) per step"}
+    # accuracy of the last step
+    Yh = A.cpu().numpy()
+    Th = T.cpu().numpy()
+    Y = np.tril(Yh, -1)
+    Y[np.arange(b), np.arange(b)] = 1.0
+    R = np.triu(Yh[:b])
+    QR = np.vstack([R, np.zeros((m - b, b))])
+    QR = QR - Y @ (Th @ (Y.T @ QR))
+    bwd = float(np.linalg.norm(QR - A0h) / np.linalg.norm(A0h))
+    E = np.eye(m, b) - Y @ (Th @ Y[:b].T)
+    orth = float(np.linalg.norm(E.T @ E - np.eye(b)))
+
+    e2e = None
+    if not args.no_e2e:
+        pin = torch.empty((b, m), dtype=torch.float64, pin_memory=True)
+        hv = pin.numpy().T
+        Wh = np.zeros((b, b), order="F")
+        Th2 = np.zeros((b, b), order="F")
+        tt, reps = 0.0, 0
+        for it in range(args.warmup + max(args.steps, 20)):
+            hv[:] = A0h
+            t0 = time.perf_counter()
+            cm.hh_recon_qr(hv, Wh, Th2)
+            dt = time.perf_counter() - t0
+            if it >= args.warmup:
+                tt += dt
+                reps += 1
+        e2e = {"value": ctx.world * f * reps / tt / 1e9, "unit": "GFLOP/s",
+               "h2d_bytes_per_step": 8 * m * b, "d2h_bytes_per_step": 8 * (m * b + 2 * b * b)}
+    cpu = None
+    if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu:
+        gf, reps, cores = cpu_tsqr_hr(args, m, b)
+        cpu = {"value": gf, "unit": "GFLOP/s", "cores": cores, "kind": "port",
+               "sample": f"hh_recon_qr call sequence (dgeqrf, dorgqr, signed LU, dtrsm) on {m}x{b}, "
+                         f"{reps} runs in ~{args.cpu_seconds:.0f} s"}
+    line = base_line(args, ctx, "TSQR-HR GFLOP/s (2mb^2 - 2/3 b^3 per panel)", value, "GFLOP/s",
+                     t_max / args.steps, "f64",
+                     {"workload": f"hh_recon_qr {m}x{b} float64 N(0,1) (PCG64 seed 0)", "m": m, "b": b,
+                      "parallelism": f"replicas x{ctx.world}",
+                      "l2": "512 MB buffer written between steps (input 4 MB < L2)"})
+    line.update({"clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof,
+                 "cpu_baseline": cpu,
+                 "accuracy": {"backward_error": bwd, "orthogonality": orth, "bound": 1e-13}})
+    return line
+
+
+# ----------------------------------------------------------------- forms
+def wl_forms(args, ctx):
+    import torch
+    cm = ctx.cm
+    m, n, b = args.m, args.n, args.b
+    forms = [f for f in args.forms.split(",") if f]
+    _preload_linalg()
+    rng = np.random.default_rng(args.seed)
+    U = haar_gpu(rng, m, n, ctx.dev)
+    V = haar_gpu(rng, n, n, ctx.dev)
+    B = cm.colmajor(torch.from_numpy(rng.standard_normal((m, 16))).to(ctx.dev))
+    cases = []
+    head = None
+    total_launches = 0
+    clk_all = []
+    for smin in (1e-10, 1e-3):
+        s = torch.logspace(0, np.log10(smin), n, dtype=torch.float64, device=ctx.dev)
+        A0 = cm.colmajor((U * s[None, :]) @ V.t())
+        A = torch.empty_like(A0.t()).t()
+        x64 = None
+        for form in sorted(forms, key=lambda f: f != "fp64"):
+            def step():
+                A.copy_(A0)
+                cm.QR_2D_pipe(A, b, precision=form)
+            for _ in range(args.warmup):
+                step()
+            torch.cuda.synchronize()
+            dom = {"fp64": ["gemm_tn", "gemm_nn"], "ozaki": ["oz_tn", "oz_nn"], "fp32": ["f32"]}[form]
+            t_max, launches, prof, clk = ctx.timed(step, args.steps, dom)
+            total_launches += launches
+            clk_all.append(clk)
+            tf = qr_flops(m, n) * args.steps / (t_max / 1e3) / 1e12
+            bwd = sampled_backward_error(cm, A0, A, b)
+            dom_ms = sum(prof[c][0] for c in dom)
+            dom_tf = sum(prof[c][1] for c in dom) / (dom_ms / 1e3) / 1e12 if dom_ms else None
+            # least squares, 16 right-hand sides, FP64 refinement
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            X, st = cm.ls_solve(A0, B, b, precision=form, max_refine=20)
+            e1.record()
+            torch.cuda.synchronize()
+            ls_ms = e0.elapsed_time(e1)
+            Rr = B - A0 @ X
+            opt = float(torch.linalg.norm(A0.t() @ Rr) / (torch.linalg.norm(A0) * torch.linalg.norm(Rr)))
+            if form == "fp64":
+                x64 = X.clone()
+                r64 = float(torch.linalg.norm(Rr))
+            rec = {"sigma_min": smin, "form": form, "qr_tflops": tf, "qr_ms": t_max / args.steps,
+                   "dominant_kernel_tflops": dom_tf, "backward_error_sampled": bwd, "ls_ms": ls_ms,
+                   "refine_steps": st["steps"], "last_correction": st["last_change"],
+                   "normal_eq_residual": opt}
+            if x64 is not None:
+                rec["x_rel_diff_vs_fp64"] = float(torch.linalg.norm(X - x64) / torch.linalg.norm(x64))
+                rec["resid_rel_diff_vs_fp64"] = abs(float(torch.linalg.norm(Rr)) - r64) / r64
+            cases.append(rec)
+            if smin == 1e-10 and form == forms[0]:
+                head = (tf, t_max / args.steps, form, prof, dom)
+            del X, Rr
+        del A0, A
+    tf, ms, form, prof, dom = head
+    roof = None
+    if form == "ozaki":
+        pk = measured_peaks().get("bf16_tflops_sustained", 1700.0) / 28.0
+        dom_ms = sum(prof[c][0] for c in dom)
+        ach = sum(prof[c][1] for c in dom) / (dom_ms / 1e3) / 1e12 if dom_ms else None
+        roof = {"bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s",
+                "frac": ach / pk if ach else None, "traffic": None,
+                "kernel": "k_oz_mma", "peak_source": "bf16_tflops_sustained / 28 (of measured)"}
+    line = base_line(args, ctx, "CAQR TFLOP/s by precision form (FP64-equivalent, 2mn^2 - 2/3 n^3)",
+                     tf * ctx.world, "TFLOP/s", ms, f"{form} trailing update, f64 panels",
+                     {"workload": f"CAQR {m}x{n} b={b}, A=U diag(logspace(0,-10|-3,n)) V^T, U,V Haar "
+                                  f"(PCG64 seed {args.seed}); LS with 16 N(0,1) RHS refined in FP64",
+                      "m": m, "n": n, "b": b, "forms": forms, "headline": f"{form} at sigma_min 1e-10",
+                      "l2": "input 4 GiB > L2"})
+    line.update({"clocks": clk_all[0] if clk_all else None, "clocks_all": clk_all, "e2e": None,
+                 "gpu_launches": total_launches, "roofline": roof, "cpu_baseline": None, "cases": cases})
+    return line
+
+
+# ----------------------------------------------------------------- batched
+def batched_sizes(count, seed=3, m_lo=256, m_hi=262144, widths=(8, 16, 32, 64, 128)):
+    """(m_i, n_i) per problem: PCG64 streams from SeedSequence(seed).spawn(count),
+    m_i = round(exp(U(ln m_lo, ln m_hi))), n_i uniform over widths, m_i >= n_i."""
+    out = []
+    for ss in np.random.SeedSequence(seed).spawn(count):
+        r = np.random.default_rng(ss)
+        m = int(round(np.exp(r.uniform(np.log(m_lo), np.log(m_hi)))))
+        n = int(r.choice(widths))
+        out.append((max(m, n), n))
+    return out
+
+
+def wl_batched(args, ctx):
+    import torch
+    cm = ctx.cm
+    count = args.count
+    sizes = batched_sizes(count, seed=3)
+    al = 32                                     # 256-byte aligned problem starts
+    offA, offB, ta, tb = [], [], 0, 0
+    for m, n in sizes:
+        offA.append(ta)
+        offB.append(tb)
+        ta += (m * n + al - 1) // al * al
+        tb += (m + al - 1) // al * al
+    g = torch.Generator(device=ctx.dev)
+    g.manual_seed(3)
+    A0 = torch.randn(ta, dtype=torch.float64, device=ctx.dev, generator=g)
+    B0 = torch.randn(tb, dtype=torch.float64, device=ctx.dev, generator=g)
+    Ap, Bp = A0.clone(), B0.clone()
+    As = [Ap[o:o + m * n].view(n, m).t() for o, (m, n) in zip(offA, sizes)]
+    Bs = [Bp[o:o + m].view(1, m).t() for o, (m, n) in zip(offB, sizes)]
+    xidx = torch.cat([torch.arange(o, o + n) for o, (m, n) in zip(offB, sizes)]).to(ctx.dev)
+
+    tuned = {"nstreams": 16, "leaf_rows": 64, "source": "default"}
+    if not args.no_tune:
+        from candmc_gb300 import autotune
+        ns = min(512, count)
+
+        def make_batch():
+            sA = [a.clone().t().contiguous().t() for a in As[:ns]]
+            sB = [bb.clone() for bb in Bs[:ns]]
+            for a, o, (m, n) in zip(sA, offA, sizes):
+                a.copy_(A0[o:o + m * n].view(n, m).t())
+            for bb, o, (m, n) in zip(sB, offB, sizes):
+                bb.copy_(B0[o:o + m].view(1, m).t())
+            return sA, sB
+        best, trials = autotune.tune_batched(make_batch, [m for m, _ in sizes[:ns]],
+                                             [n for _, n in sizes[:ns]])
+        tuned = dict(best, source=f"autotune on the first {ns} problems", trials=len(trials))
+    cm.set_tuning("leaf_rows", tuned["leaf_rows"])
+    use_graph = not args.no_graph
+
+    def step():
+        Ap.copy_(A0)
+        Bp.copy_(B0)
+        cm.batched_ls(As, Bs, nstreams=tuned["nstreams"], use_graph=use_graph)
+
+    cm.batched_ls(As, Bs, nstreams=tuned["nstreams"])   # eager run first (kernel attributes)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    classes = ["panel_leaf", "panel_y", "small", "gemm_tn", "gemm_nn", "reduce"]
+    t_max, launches, prof, clk = ctx.timed(step, args.steps, classes)
+    solves = ctx.world * count * args.steps / (t_max / 1e3)
+    f = sum(qr_flops(m, n) for m, n in sizes)
+    by = sum(16.0 * m * n for m, n in sizes)
+    roof = fp64_roof(prof, ["panel_leaf", "panel_y"], "k_hr4_leaf_tree + k_hr4_form_y", t_max)
+    hbm = measured_peaks().get("hbm_gbs", 6778.0)
+    roof["step_fp64_tflops"] = f * args.steps / (t_max / 1e3) / 1e12
+    roof["hbm"] = {"achieved_gbs": by * args.steps / (t_max / 1e3) / 1e9, "peak_gbs": hbm,
+                   "frac": by * args.steps / (t_max / 1e3) / 1e9 / hbm,
+                   "note": "algorithmic bytes 16 m n per problem (read A, write Y)"}
+    # accuracy on a sample of problems against LAPACK lstsq (numpy)
+    torch.cuda.synchronize()
+    rs = np.random.default_rng(0)
+    small = [i for i, (m, n) in enumerate(sizes) if m <= 65536]
+    errs = []
+    for i in rs.choice(small, size=min(12, len(small)), replace=False):
+        m, n = sizes[i]
+        Ah = A0[offA[i]:offA[i] + m * n].view(n, m).t().cpu().numpy()
+        bh = B0[offB[i]:offB[i] + m].cpu().numpy()
+        xo = np.linalg.lstsq(Ah, bh, rcond=None)[0]
+        x = Bp[offB[i]:offB[i] + n].cpu().numpy()
+        errs.append(float(np.linalg.norm(x - xo) / np.linalg.norm(xo)))
+
+    e2e = None
+    if not args.no_e2e:
+        try:
+            hA = torch.empty(ta, dtype=torch.float64, pin_memory=True)
+            hB = torch.empty(tb, dtype=torch.float64, pin_memory=True)
+            hA.copy_(A0)
+            hB.copy_(B0)
+            hx = torch.empty(xidx.numel(), dtype=torch.float64, pin_memory=True)
+            tt = 0.0
+            for it in range(1 + args.steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                Ap.copy_(hA, non_blocking=True)
+                Bp.copy_(hB, non_blocking=True)
+                cm.batched_ls(As, Bs, nstreams=tuned["nstreams"], use_graph=use_graph)
+                hx.copy_(Bp[xidx], non_blocking=True)
+                torch.cuda.synchronize()
+                if it >= 1:
+                    tt += time.perf_counter() - t0
+            e2e = {"value": ctx.world * count * args.steps / tt, "unit": "solves/s",
+                   "h2d_bytes_per_step": 8 * (ta + tb), "d2h_bytes_per_step": 8 * xidx.numel()}
+            del hA, hB
+        except RuntimeError as ex:
+            e2e = {"value": None, "unit": "solves/s", "h2d_bytes_per_step": 8 * (ta + tb),
+                   "d2h_bytes_per_step": 8 * xidx.numel(), "error": str(ex)[:200]}
+    cpu = None
+    if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu:
+        tasks = [(m, n, 1000 + i) for i, (m, n) in enumerate(sizes)]
+        rate, done, cores = cpu_ls_rate(tasks, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "solves/s", "cores": cores, "kind": "port",
+               "sample": f"first {done} problems (same size distribution), reference call sequence "
+                         "(hh_recon_qr + update_A on [A|b] + dtrsm), one single-threaded process per core"}
+    line = base_line(args, ctx, "batched least squares solves/s", solves, "solves/s", t_max / args.steps,
+                     "f64",
+                     {"workload": f"{count} LS problems, m log-uniform [256, 262144], n in "
+                                  "{8,16,32,64,128}, A,b ~ N(0,1) on the device (Philox seed 3)",
+                      "problems": count, "tuning": tuned, "graph": use_graph,
+                      "l2": f"inputs {8 * ta / 1e9:.0f} GB > L2"})
+    line.update({"clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+                 "accuracy": {"x_rel_err_vs_lstsq_max": max(errs) if errs else None, "sampled": len(errs),
+                              "bound": 1e-12}})
+    return line
+
+
+# ----------------------------------------------------------------- serve
+def serve_trace(args, count, rate):
+    from candmc_gb300.serve import poisson_trace
+    return poisson_trace(count, rate, seed=4, m_lo=512, m_hi=1048576, widths=(16, 32, 64, 128, 256))
+
+
+def wl_serve(args, ctx):
+    import torch
+    cm = ctx.cm
+    from candmc_gb300.serve import LSServer, latency_summary, replay
+    M, N = 1048576, 256
+    ss = np.random.SeedSequence(4).spawn(3)
+    pools = []
+    for k in range(2):
+        t = torch.empty((N, M), dtype=torch.float64, pin_memory=True)
+        np.random.default_rng(ss[k]).standard_normal(out=t.numpy())
+        pools.append(t.numpy().T)                # Fortran view M x N
+    tb = torch.empty(M, dtype=torch.float64, pin_memory=True)
+    np.random.default_rng(ss[2]).standard_normal(out=tb.numpy())
+    bpool = tb.numpy()
+
+    def inputs(i, m, n):
+        return pools[i % 2][:m, :n], bpool[:m]
+
+    rates = [float(r) for r in args.rates.split(",")]
+    budget = args.budget_gb * 1e9
+    form = args.form
+    results = []
+    clk, launches = None, 0
+    with LSServer(budget_bytes=budget, workers=args.workers, precision=form) as srv:
+        warm = serve_trace(args, 24, 1e6)
+        replay(srv, warm, inputs)
+        for k, rate in enumerate(rates):
+            trace = serve_trace(args, args.count, rate)
+            torch.cuda.synchronize()
+            sampler = ClockSampler(gpu_id_for_smi(ctx.local)) if k == len(rates) - 1 else None
+            l0 = ctx.lib.candmc_launch_count()
+            xs, infos = replay(srv, trace, inputs)
+            launches += ctx.lib.candmc_launch_count() - l0
+            if sampler:
+                clk = sampler.stop()
+            summ = latency_summary(infos)
+            summ["rate"] = rate
+            summ["peak_in_flight"] = srv.stats()["peak_in_flight"]
+            results.append(summ)
+        st = srv.stats()
+    # accuracy on sampled requests of the last trace against LAPACK lstsq (numpy)
+    errs = []
+    for i, (_, m, n) in enumerate(trace):
+        if m <= 65536 and len(errs) < 12:
+            A, bvec = inputs(i, m, n)
+            xo = np.linalg.lstsq(np.asarray(A), bvec, rcond=None)[0]
+            errs.append(float(np.linalg.norm(xs[i] - xo) / np.linalg.norm(xo)))
+    # plain FP64 per-request path on the same (highest-rate) trace
+    with LSServer(budget_bytes=budget, workers=1, precision="fp64") as srv:
+        replay(srv, serve_trace(args, 8, 1e6), inputs)
+        _, infos64 = replay(srv, trace, inputs)
+    base = latency_summary(infos64)
+    cpu = None
+    if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu:
+        tasks = [(m, n, 2000 + i) for i, (_, m, n) in enumerate(trace)]
+        rate, done, cores = cpu_ls_rate(tasks, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "solves/s", "cores": cores, "kind": "port",
+               "sample": f"first {done} requests of the trace, reference call sequence, one "
+                         "single-threaded process per core (throughput only)"}
+    top = results[-1]
+    mean_in = float(np.mean([8.0 * (m * n + m) for _, m, n in trace]))
+    mean_out = float(np.mean([8.0 * n for _, m, n in trace]))
+    line = base_line(args, ctx, "least-squares requests solves/s (continuous batching, refined to 1e-12)",
+                     top["solves_per_s"] * ctx.world, "solves/s", 1e3 / top["solves_per_s"],
+                     f"{form} trailing update, f64 panels and refinement",
+                     {"workload": "Poisson arrivals (seed 4), m log-uniform [512, 1048576], n in "
+                                  "{16,32,64,128,256}, A,b ~ N(0,1) host buffers",
+                      "requests_per_rate": args.count, "rates": rates, "workers": args.workers,
+                      "budget_gb": args.budget_gb, "form": form})
+    line.update({"clocks": clk, "gpu_launches": launches,
+                 "e2e": {"value": top["solves_per_s"] * ctx.world, "unit": "solves/s",
+                         "h2d_bytes_per_step": mean_in, "d2h_bytes_per_step": mean_out,
+                         "note": "every request is copied in from host memory and x copied back"},
+                 "latency": results, "fp64_per_request": base,
+                 "server": {"peak_bytes_reserved": st["peak_bytes_reserved"],
+                            "peak_in_flight": st["peak_in_flight"]},
+                 "roofline": None, "cpu_baseline": cpu,
+                 "accuracy": {"x_rel_err_vs_lstsq_max": max(errs) if errs else None, "sampled": len(errs),
+                              "bound": 1e-12}})
+    return line
+
+
+# ----------------------------------------------------------------- main
+DEFAULTS = {
+    "caqr": {"n": 16384, "b": 128, "form": "ozaki", "seed": 1},
+    "tsqr_hr": {"m": 8192, "b": 64, "seed": 0},
+    "forms": {"m": 32768, "n": 16384, "b": 128, "seed": 2, "form": "ozaki"},
+    "batched": {"count": 4096, "seed": 3},
+    "serve": {"count": 400, "form": "fp32", "seed": 4},
+}
+
+
+def main():
+    args = parse()
+    for k, v in DEFAULTS[args.workload].items():
+        if getattr(args, k) is None:
+            setattr(args, k, v)
+    if args.b is None:
+        args.b = 128
+    if args.form is None:
+        args.form = "ozaki"
+    if args.impl == "reference":
+        return run_reference(args)
+    ctx = Ctx(args)
+    fn = {"caqr": wl_caqr, "tsqr_hr": wl_tsqr_hr, "forms": wl_forms, "batched": wl_batched,
+          "serve": wl_serve}[args.workload]
+    line = fn(args, ctx)
+    if ctx.rank == 0:
         print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    if ctx.dist:
+        ctx.dist.destroy_process_group()
     return 0
 
 

@@ -40,12 +40,21 @@ SIGNATURES = {
                         ctypes.c_double, _vp, _vp],
     "candmc_batched_ls": [_i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp],
     "candmc_set_tuning": [ctypes.c_char_p, _i64],
+    "candmc_server_create": [ctypes.c_double, _int, _int, _i64, _int, ctypes.c_double, _vp],
+    "candmc_server_submit": [_vp, _vp, _i64, _i64, _i64, _vp, _vp, ctypes.c_double, _vp],
+    "candmc_server_wait": [_vp, _i64, ctypes.c_double, _vp],
+    "candmc_server_now": [_vp],
+    "candmc_server_stats": [_vp, _vp],
+    "candmc_server_destroy": [_vp],
+    "candmc_ls_request_bytes": [_i64, _i64, _i64, _int],
+    "candmc_mem_high_water": [_int, _vp],
     "candmc_launch_count": [],
     "candmc_profile_begin": [ctypes.c_uint],
     "candmc_profile_end": [_int, _vp, _vp, _vp],
 }
 _RESTYPES = {"candmc_status_string": ctypes.c_char_p, "candmc_last_error": ctypes.c_char_p,
-             "candmc_launch_count": ctypes.c_longlong}
+             "candmc_launch_count": ctypes.c_longlong, "candmc_server_now": ctypes.c_double,
+             "candmc_ls_request_bytes": ctypes.c_int64}
 
 # kernel classes of candmc_profile_begin / candmc_profile_end (CANDMC_KCLASS_*)
 KCLASS = {"gemm_tn": 0, "gemm_nn": 1, "reduce": 2, "panel_leaf": 3, "panel_y": 4, "small": 5,

@@ -47,7 +47,24 @@ struct StreamPool {
 
 static StreamPool g_pool[64];
 static std::mutex g_graph_mu;
-static std::map<std::vector<int64_t>, cudaGraphExec_t> g_graphs;
+struct CachedGraph {
+  cudaGraphExec_t exec;
+  long long kernels;   // kernel nodes: launches per replay
+};
+static std::map<std::vector<int64_t>, CachedGraph> g_graphs;
+
+static long long kernel_nodes(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+  long long k = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
 
 static int batched_issue(int64_t nprob, const int64_t* m, const int64_t* n, double* const* A,
                          const int64_t* lda, double* const* B, int nstreams, cudaStream_t s) {
@@ -150,10 +167,14 @@ extern "C" int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t*
   cudaStream_t cs = g_pool[dev].get(63);
   if (!cs) return set_error(CANDMC_ERR_CUDA, "capture stream");
   cudaGraphExec_t exec = nullptr;
+  long long nkern = 0;
   {
     std::lock_guard<std::mutex> g(g_graph_mu);
     auto it = g_graphs.find(key);
-    if (it != g_graphs.end()) exec = it->second;
+    if (it != g_graphs.end()) {
+      exec = it->second.exec;
+      nkern = it->second.kernels;
+    }
   }
   if (!exec) {
     // kernel attributes are set by an eager run first (not a stream operation)
@@ -166,11 +187,15 @@ extern "C" int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t*
       return rc;
     }
     CANDMC_CK(e);
+    // the capture counted its launches although nothing ran; each replay
+    // counts the graph's kernel nodes instead
+    nkern = kernel_nodes(graph);
+    count_launches(-nkern);
     e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     CANDMC_CK(e);
     std::lock_guard<std::mutex> g(g_graph_mu);
-    g_graphs[key] = exec;
+    g_graphs[key] = {exec, nkern};
   }
   cudaEvent_t e0, e1;
   CANDMC_CK(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
@@ -178,6 +203,7 @@ extern "C" int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t*
   cudaError_t e = cudaEventRecord(e0, s);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, e0, 0);
   if (e == cudaSuccess) e = cudaGraphLaunch(exec, cs);
+  if (e == cudaSuccess) count_launches(nkern);
   if (e == cudaSuccess) e = cudaEventRecord(e1, cs);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(s, e1, 0);
   cudaEventDestroy(e0);

@@ -38,9 +38,9 @@ int cuda_status(cudaError_t e, const char* where) {
 // pool instead of returning it to the driver at every synchronisation, so a
 // repeated factorization reuses its scratch without re-mapping memory.
 static void ensure_pool() {
-  static bool done[64] = {};
+  static std::atomic<bool> done[64] = {};
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev].load()) return;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
     uint64_t thr = ~0ull;
@@ -218,17 +218,28 @@ static int check_form(int precision, int64_t b, bool* pair) {
 }
 
 // High-priority, non-blocking side stream per device for the lookahead panels.
+// One lookahead stream per host thread and device, so that factorizations
+// issued concurrently from several threads (the request server's workers) do
+// not queue their panels behind one another.
+struct PanelStreams {
+  cudaStream_t sp[64] = {};
+  ~PanelStreams() {
+    for (auto s : sp)
+      if (s) cudaStreamDestroy(s);
+  }
+};
+
 static cudaStream_t panel_stream() {
-  static cudaStream_t sp[64] = {};
+  static thread_local PanelStreams ps;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  if (!sp[dev]) {
+  if (!ps.sp[dev]) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    if (cudaStreamCreateWithPriority(&sp[dev], cudaStreamNonBlocking, hi) != cudaSuccess)
-      sp[dev] = nullptr;
+    if (cudaStreamCreateWithPriority(&ps.sp[dev], cudaStreamNonBlocking, hi) != cudaSuccess)
+      ps.sp[dev] = nullptr;
   }
-  return sp[dev];
+  return ps.sp[dev];
 }
 
 struct EventRing {
@@ -393,6 +404,7 @@ const char* candmc_status_string(int status) {
     case CANDMC_ERR_TIMEOUT: return "device wait timed out";
     case CANDMC_ERR_NUMERIC: return "non-finite value or zero pivot";
     case CANDMC_ERR_NODEV: return "no usable CUDA device";
+    case CANDMC_ERR_CANCELLED: return "request cancelled at server shutdown";
     default: return "unknown status";
   }
 }

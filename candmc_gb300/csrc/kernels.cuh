@@ -1,5 +1,7 @@
 // Host-side launchers shared between the translation units of the library.
 #pragma once
+#include <atomic>
+
 #include "common.cuh"
 
 namespace candmc {
@@ -9,6 +11,8 @@ namespace candmc {
 // CANDMC_KCLASS_* values of the public header.
 constexpr int kProfClasses = 16;
 void count_launch();
+void count_launches(long long n);   // kernels of a replayed CUDA graph
+long long launch_total();
 bool prof_on(int cls);
 class ProfScope {
  public:

@@ -249,7 +249,7 @@ extern "C" int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t 
   CANDMC_RET(rel.alloc(sizeof(double) * nrhs, s));
   std::vector<double> hrel(nrhs);
   int it = 0;
-  double first = -1.0, last = 0.0;
+  double first = -1.0, last = 0.0, prev = HUGE_VAL;
   for (; it < max_refine; ++it) {
     CANDMC_RET(ts_gemm(false, A, lda, X, ldx, m, n, nrhs, -1.0, 1.0, B, ldb, Rres.d(), m, s));
     CANDMC_RET(ts_gemm(true, A, lda, Rres.d(), m, n, m, nrhs, 1.0, 0.0, nullptr, 0, Sv.d(), n, s));
@@ -257,7 +257,6 @@ extern "C" int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t 
     CANDMC_RET(trsm_upper(F.d(), m, n, Dinv.d(), w, Sv.d(), n, nrhs, false, s));
     {
       ProfScope ps(CANDMC_KCLASS_SMALL, 0.0, s);
-      k_add<<<(unsigned)((n * nrhs + 255) / 256), 256, 0, s>>>(X, ldx, Sv.d(), n, n, nrhs);
       k_rel_change<<<(unsigned)nrhs, 256, 0, s>>>(Sv.d(), n, X, ldx, n, rel.d());
       CANDMC_CK(cudaGetLastError());
     }
@@ -265,7 +264,16 @@ extern "C" int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t 
     CANDMC_CK(cudaStreamSynchronize(s));
     last = *std::max_element(hrel.begin(), hrel.end());
     if (first < 0.0) first = last;
-    if (!(last == last)) break;   // NaN: diverged
+    // the iteration contracts only while kappa(A)^2 u_R < 1: a correction
+    // that is not smaller than the previous one (or not finite) is dropped
+    // and the refinement ends with the current X
+    if (!(last == last) || (last >= prev && last > tol)) break;
+    {
+      ProfScope ps(CANDMC_KCLASS_SMALL, 0.0, s);
+      k_add<<<(unsigned)((n * nrhs + 255) / 256), 256, 0, s>>>(X, ldx, Sv.d(), n, n, nrhs);
+      CANDMC_CK(cudaGetLastError());
+    }
+    prev = last;
     if (last <= tol) {
       ++it;
       break;

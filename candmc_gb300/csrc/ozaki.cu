@@ -544,7 +544,7 @@ static int launch_slice_krow(SliceSrc src, int64_t n0, int64_t Nvalid, int64_t K
 
 static int launch_oz(const OzArgs& a, unsigned gm, unsigned gn, unsigned gk, int cls, double flops,
                      cudaStream_t s) {
-  static bool attr = false;
+  static std::atomic<bool> attr{false};
   if (!attr) {
     CANDMC_CK(cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
     attr = true;

@@ -23,6 +23,10 @@ static std::vector<ProfRec> g_prof[kProfClasses];
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+long long launch_total() { return g_launches.load(); }
+
 bool prof_on(int cls) { return (g_prof_mask >> cls) & 1u; }
 
 ProfScope::ProfScope(int cls, double work, cudaStream_t s) : cls_(cls), work_(work), s_(s) {

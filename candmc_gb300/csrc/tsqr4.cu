@@ -590,7 +590,7 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   a.Vw = vw.d(); a.Tl = tl.d(); a.Rn = rn.d(); a.Qn = qn.d();
   a.cnt = static_cast<unsigned*>(cnt.p);
   a.T = T; a.ldT = ldT; a.W = W; a.ldW = ldW; a.Uinv = uinv.d(); a.status = d_status;
-  static bool attr = false;
+  static std::atomic<bool> attr{false};
   if (!attr) {
     CANDMC_CK(cudaFuncSetAttribute(k_hr4_leaf_tree, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    200 * 1024));

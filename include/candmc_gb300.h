@@ -185,8 +185,11 @@ int candmc_QR_2D_pipe(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, i
  * resident for the residuals), X0 = R^-1 (Q^T B)[0:n] with Q applied in FP64,
  * then up to max_refine FP64 refinement steps by corrected semi-normal
  * equations (r = B - A X, X += R^-1 R^-T A^T r) until the largest per-column
- * max|dX| / max|X| is <= tol.  stats (nullable, 4 doubles): steps taken, last
- * and first relative correction, device status. */
+ * max|dX| / max|X| is <= tol.  The iteration contracts while
+ * kappa(A)^2 * u_R < 1 (u_R: the unit roundoff of R's form); a correction
+ * that is not smaller than the one before is not applied and ends the
+ * refinement.  stats (nullable, 4 doubles): corrections applied, last and
+ * first relative correction, device status. */
 int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t n, const double* B, int64_t ldb,
                     int64_t nrhs, double* X, int64_t ldx, int64_t b, int precision, int max_refine,
                     double tol, double* stats, void* stream);
@@ -204,6 +207,51 @@ int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t* n, double*
 
 /* tuning knobs: "leaf_rows" (target rows per TSQR leaf, 32..256, default 64) */
 int candmc_set_tuning(const char* key, int64_t value);
+
+/* ---- least-squares request server (no counterpart in the reference) ---------
+ * Continuous batching of single-RHS least-squares requests on one GPU.
+ * nworkers host threads, each with its own CUDA stream, take requests in
+ * arrival order; a request is admitted once its arrival time has come, a
+ * worker is idle and its device-memory estimate (candmc_ls_request_bytes)
+ * fits beside the admitted ones within budget_bytes.  Each admitted request is
+ * copied in from HOST memory, solved by candmc_ls_solve (A, Y\R, T and R stay
+ * resident across the refinement steps) and x is copied back out.  Requests
+ * run concurrently on the workers' streams; the kernels of one request do not
+ * depend on what else runs, so each result is the same alone and in a mix.
+ *
+ * candmc_server_create: precision form, panel width b and the refinement
+ *   controls of candmc_ls_solve; *out receives the handle.
+ * candmc_server_submit: A (m x n, ld lda), bvec (m) and x (n) are host
+ *   pointers that must stay valid until the request completes; arrival_s is
+ *   the earliest admission time on the server clock (candmc_server_now; pass
+ *   a time <= now for "at once").  A request whose estimate exceeds the whole
+ *   budget fails with CANDMC_ERR_ALLOC at once.  *ticket identifies it.
+ * candmc_server_wait: waits up to timeout_s seconds (< 0: no limit) for the
+ *   request; returns CANDMC_ERR_TIMEOUT if it has not completed, else the
+ *   request's own status.  info (nullable, 8 doubles): status, arrival, admit
+ *   and completion times (s, server clock), refinement steps, last relative
+ *   correction, device bytes reserved, worker index.
+ * candmc_server_stats (8 doubles): bytes reserved now, peak bytes reserved,
+ *   requests completed, requests in flight now, peak in flight, requests
+ *   pending, budget, workers.
+ * candmc_server_destroy: lets running requests finish, cancels pending ones
+ *   (status CANDMC_ERR_CANCELLED) and joins the workers. */
+#define CANDMC_ERR_CANCELLED 7   /* request dropped when the server shut down */
+int candmc_server_create(double budget_bytes, int nworkers, int precision, int64_t b, int max_refine,
+                         double tol, void** out);
+int candmc_server_submit(void* server, const double* A, int64_t lda, int64_t m, int64_t n,
+                         const double* bvec, double* x, double arrival_s, int64_t* ticket);
+int candmc_server_wait(void* server, int64_t ticket, double timeout_s, double* info);
+double candmc_server_now(void* server);
+int candmc_server_stats(void* server, double* out);
+int candmc_server_destroy(void* server);
+/* device bytes a candmc_ls_solve of an m x n problem with one right-hand side
+ * reserves at most (inputs, factor, T factors, residual vectors and the
+ * largest transient workspace of the panel and trailing-update kernels) */
+int64_t candmc_ls_request_bytes(int64_t m, int64_t n, int64_t b, int precision);
+/* high-water mark of the device's default memory pool (bytes in use); reset
+ * != 0 restarts it from the current use */
+int candmc_mem_high_water(int reset, uint64_t* bytes);
 
 #ifdef __cplusplus
 }

@@ -152,3 +152,29 @@ def QR_2D_lapack(A, b):
         else:
             break
     return A
+
+
+def ls_solve_lapack(A, B, b):
+    """Least squares by the reference's own call sequence on a 1 x 1 grid:
+    hh_recon_qr on each b-column panel of A (hh_recon.cxx:129-321), update_A
+    of the panel's Q^T on the rest of [A | B] (qr_2d.cxx:124-177, 224-282),
+    then X = R^-1 (Q^T B)[0:n] by dtrsm.  A (m x n), B (m x r); returns X."""
+    m, n = A.shape
+    B = np.asarray(B, dtype=np.float64).reshape(m, -1)
+    r = B.shape[1]
+    Aug = np.empty((m, n + r), order="F")
+    Aug[:, :n] = A
+    Aug[:, n:] = B
+    Af = _flat(Aug)
+    lda = m
+    r0 = 0
+    while r0 < n:
+        bb = min(b, n - r0)
+        off = r0 * lda + r0
+        W = hh_recon_qr_lapack(Af, lda, off, m - r0, bb)
+        upd_A_lapack(Af, lda, off, off + bb * lda, m - r0, n + r - r0 - bb, bb, W)
+        r0 += bb
+    R = np.array(np.triu(Aug[:n, :n]), order="F")
+    X = np.array(Aug[:n, n:], order="F")
+    dtrsm("L", "U", "N", "N", n, r, 1.0, R, 0, n, X, 0, n)
+    return X

@@ -65,8 +65,10 @@ def test_batched_graph_capture_and_replay(cm):
             a.copy_(a0)
         for bb, b0 in zip(Bs, B0):
             bb.copy_(b0)
+        l0 = cm.lib().candmc_launch_count()
         xs = cm.batched_ls(As, Bs, nstreams=4, use_graph=True)
         torch.cuda.synchronize()
+        assert cm.lib().candmc_launch_count() - l0 >= 3 * len(host)   # replays count their kernels
         check(host, xs)
 
 

@@ -14,6 +14,7 @@ import pytest
 from oracle import candmc_oracle as co
 from oracle import fixtures as fx
 from oracle import lapack_restated as lp
+from oracle import reference_lapack as rl
 from tests.golden.make_golden import PANELS, panel_input
 
 
@@ -145,3 +146,18 @@ def test_invT_identities(golden):
     Xt = np.linalg.inv(T).T
     assert np.abs(X1 - Xt).max() < 1e-10
     assert np.abs(X2 - Xt).max() < 1e-10
+
+
+@pytest.mark.parametrize("m,n,b", [(600, 200, 64), (2000, 256, 128), (1000, 130, 128)])
+def test_reference_call_sequence_ls_matches_oracle(m, n, b):
+    """The LAPACK replay of the reference's calls (hh_recon_qr + update_A on
+    [A | B] + dtrsm), used as the CPU baseline of the least-squares
+    workloads, agrees with the restated oracle and with LAPACK's lstsq."""
+    A = fx.gaussian(m, n, 3 * m + n)
+    B = fx.gaussian(m, 2, 5)
+    X = rl.ls_solve_lapack(A, B, b)
+    Xo = co.ls_solve(A, B, b)
+    Xl = np.linalg.lstsq(A, B, rcond=None)[0]
+    scale = max(1.0, np.abs(Xl).max())
+    assert np.abs(X - Xo).max() <= 1e-12 * scale
+    assert np.abs(X - Xl).max() <= 1e-12 * scale
