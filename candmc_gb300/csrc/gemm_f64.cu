@@ -17,14 +17,18 @@
 
 namespace candmc {
 
-constexpr int TM = 64, TN = 64, TK = 16;
+constexpr int TK = 16;
 
-// out(i, j) = sum_{k in [k0, k1)} opA(i, k) * opB(k, j), 64 x 64 tile per CTA.
+// out(i, j) = sum_{k in [k0, k1)} opA(i, k) * opB(k, j), a (16 U) x (16 U)
+// tile per CTA (U = 4: 64 x 64; U = 2: 32 x 32 for the narrow products
+// inside a panel, where a 64 x 64 tile would be three quarters padding).
 // mode 0: store into out + split * split_stride (partials), ld ldo.
 // mode 1: out(i, j) -= result (out is the trailing matrix itself).
+template <int U>
 __global__ void __launch_bounds__(kThreads)
 k_gemm_f64(MatRef A, MatRef B, int64_t M, int64_t N, int64_t K, int64_t kchunk, double* out,
            int64_t ldo, int64_t split_stride, int mode) {
+  constexpr int TM = 16 * U, TN = 16 * U;
   __shared__ double sA[TK][TM + 1];
   __shared__ double sB[TK][TN + 1];
   const int tid = threadIdx.x;
@@ -32,11 +36,11 @@ k_gemm_f64(MatRef A, MatRef B, int64_t M, int64_t N, int64_t K, int64_t kchunk, 
   const int64_t i0 = (int64_t)blockIdx.x * TM, j0 = (int64_t)blockIdx.y * TN;
   const int64_t k0 = (int64_t)blockIdx.z * kchunk;
   const int64_t k1 = (k0 + kchunk < K) ? k0 + kchunk : K;
-  double acc[4][4];
+  double acc[U][U];
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < U; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) acc[u][v] = 0.0;
+    for (int v = 0; v < U; ++v) acc[u][v] = 0.0;
 
   for (int64_t kb = k0; kb < k1; kb += TK) {
     // A tile: TM x TK.  Coalesce along the stored row index.
@@ -55,25 +59,25 @@ k_gemm_f64(MatRef A, MatRef B, int64_t M, int64_t N, int64_t K, int64_t kchunk, 
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < TK; ++kk) {
-      double a[4], bb[4];
+      double a[U], bb[U];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) a[u] = sA[kk][ti + 16 * u];
+      for (int u = 0; u < U; ++u) a[u] = sA[kk][ti + 16 * u];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) bb[v] = sB[kk][tj + 16 * v];
+      for (int v = 0; v < U; ++v) bb[v] = sB[kk][tj + 16 * v];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], bb[v], acc[u][v]);
+        for (int v = 0; v < U; ++v) acc[u][v] = fma(a[u], bb[v], acc[u][v]);
     }
     __syncthreads();
   }
   double* o = out + (mode == 0 ? (int64_t)blockIdx.z * split_stride : 0);
 #pragma unroll
-  for (int u = 0; u < 4; ++u) {
+  for (int u = 0; u < U; ++u) {
     int64_t gi = i0 + ti + 16 * u;
     if (gi >= M) continue;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
+    for (int v = 0; v < U; ++v) {
       int64_t gj = j0 + tj + 16 * v;
       if (gj >= N) continue;
       if (mode == 0) o[gj * ldo + gi] = acc[u][v];
@@ -115,33 +119,47 @@ k_small_gemm(MatRef A, MatRef B, int64_t M, int64_t N, int64_t K, double alpha, 
 }
 
 // Z(i,j) = alpha * sum_k opT(i,k) * (sum_s Zp[s](k,j))   with Zp[s] nb x n (ld nb);
-// opT == nullptr: identity.  16 x 16 outputs per CTA.
+// opT == nullptr: identity.  One CTA per output column j; thread (i, g) of the
+// (nbp rows) x (256 / nbp groups) layout sums every G-th partial of row i, the
+// groups are combined in shared memory, and the product with opT splits its k
+// range over the groups the same way, so every dependent FP64 chain is about
+// nsplit / G + nb / G long instead of nsplit + nb.  The summation order is
+// fixed, so the result is deterministic.
 __global__ void __launch_bounds__(kThreads)
-k_reduce_apply(const double* Zp, int nsplit, int64_t split_stride, int nb, int64_t n, MatRef Top,
-               double alpha, double* Z, int64_t ldz) {
-  extern __shared__ double sh[];
-  double* sZ = sh;               // nb x 16 (ld nb)
-  const int ti = threadIdx.x % 16, tj = threadIdx.x / 16;
-  const int64_t i0 = (int64_t)blockIdx.x * 16, j0 = (int64_t)blockIdx.y * 16;
-  for (int idx = threadIdx.x; idx < nb * 16; idx += kThreads) {
-    int k = idx % nb, jj = idx / nb;
-    int64_t gj = j0 + jj;
-    double s = 0.0;
-    if (gj < n)
-      for (int sp = 0; sp < nsplit; ++sp) s += Zp[sp * split_stride + gj * nb + k];
-    sZ[jj * nb + k] = s;
+k_reduce_apply(const double* Zp, int nsplit, int64_t split_stride, int nb, int nbp, int64_t n,
+               MatRef Top, double alpha, double* Z, int64_t ldz) {
+  __shared__ double part[kThreads];
+  __shared__ double col[256];
+  const int G = kThreads / nbp;
+  const int i = threadIdx.x % nbp, g = threadIdx.x / nbp;
+  const int64_t jc = blockIdx.x;
+  double sacc = 0.0;
+  if (i < nb)
+    for (int sp = g; sp < nsplit; sp += G) sacc += Zp[sp * split_stride + jc * nb + i];
+  part[g * nbp + i] = sacc;
+  __syncthreads();
+  if (g == 0) {
+    double t = 0.0;
+    for (int h = 0; h < G; ++h) t += part[h * nbp + i];
+    col[i] = t;
   }
   __syncthreads();
-  int64_t gi = i0 + ti, gj = j0 + tj;
-  if (gi >= nb || gj >= n) return;
-  double acc;
+  double z;
   if (Top.p == nullptr) {
-    acc = sZ[tj * nb + gi];
+    z = (g == 0 && i < nb) ? col[i] : 0.0;
   } else {
-    acc = 0.0;
-    for (int k = 0; k < nb; ++k) acc = fma(mat_at(Top, gi, k), sZ[tj * nb + k], acc);
+    z = 0.0;
+    if (i < nb)
+      for (int k = g; k < nb; k += G) z = fma(mat_at(Top, i, k), col[k], z);
   }
-  Z[gj * ldz + gi] = alpha * acc;
+  __syncthreads();
+  part[g * nbp + i] = z;
+  __syncthreads();
+  if (g == 0 && i < nb) {
+    double t = 0.0;
+    for (int h = 0; h < G; ++h) t += part[h * nbp + i];
+    Z[jc * ldz + i] = alpha * t;
+  }
 }
 
 // Triangular inverse of an n x n matrix (ld), one column per thread.
@@ -234,6 +252,8 @@ int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top,
                    double* Z, int64_t ldz, cudaStream_t s) {
   if (nb <= 0 || n <= 0) return CANDMC_OK;
   if (nb > 256) return CANDMC_ERR_ARG;
+  const bool narrow = nb <= 32 && n <= 32;
+  const int TM = narrow ? 32 : 64, TN = TM;
   const int64_t tiles = ((nb + TM - 1) / TM) * ((n + TN - 1) / TN);
   // FP64 work per CTA is what bounds these kernels: aim at ~4 CTAs per SM,
   // with slices of at least 64 rows
@@ -251,14 +271,18 @@ int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top,
   dim3 grid((unsigned)((nb + TM - 1) / TM), (unsigned)((n + TN - 1) / TN), (unsigned)nsplit);
   {
     ProfScope ps(CANDMC_KCLASS_GEMM_TN, 2.0 * nb * n * m, s);
-    k_gemm_f64<<<grid, kThreads, 0, s>>>(Yt, C, nb, n, m, kchunk, part.d(), nb, stride, 0);
+    if (narrow)
+      k_gemm_f64<2><<<grid, kThreads, 0, s>>>(Yt, C, nb, n, m, kchunk, part.d(), nb, stride, 0);
+    else
+      k_gemm_f64<4><<<grid, kThreads, 0, s>>>(Yt, C, nb, n, m, kchunk, part.d(), nb, stride, 0);
   }
   CANDMC_CK(cudaGetLastError());
-  dim3 g2((unsigned)((nb + 15) / 16), (unsigned)((n + 15) / 16));
-  size_t sm = sizeof(double) * (size_t)nb * 16;
+  int nbp = 1;
+  while (nbp < nb) nbp <<= 1;
   {
     ProfScope ps(CANDMC_KCLASS_REDUCE, 8.0 * stride * nsplit, s);
-    k_reduce_apply<<<g2, kThreads, sm, s>>>(part.d(), (int)nsplit, stride, nb, n, Top, alpha, Z, ldz);
+    k_reduce_apply<<<(unsigned)n, kThreads, 0, s>>>(part.d(), (int)nsplit, stride, nb, nbp, n, Top, alpha,
+                                                    Z, ldz);
   }
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
@@ -268,9 +292,13 @@ int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top,
 int gemm_nn_sub(double* C, int64_t ldc, MatRef Y, const double* Z, int64_t ldz, int64_t m, int64_t n,
                 int nb, cudaStream_t s) {
   if (m <= 0 || n <= 0 || nb <= 0) return CANDMC_OK;
-  dim3 grid((unsigned)((m + TM - 1) / TM), (unsigned)((n + TN - 1) / TN), 1);
+  const int T = n <= 32 ? 32 : 64;
+  dim3 grid((unsigned)((m + T - 1) / T), (unsigned)((n + T - 1) / T), 1);
   ProfScope ps(CANDMC_KCLASS_GEMM_NN, 2.0 * m * n * nb, s);
-  k_gemm_f64<<<grid, kThreads, 0, s>>>(Y, mref(Z, ldz), m, n, nb, nb, C, ldc, 0, 1);
+  if (T == 32)
+    k_gemm_f64<2><<<grid, kThreads, 0, s>>>(Y, mref(Z, ldz), m, n, nb, nb, C, ldc, 0, 1);
+  else
+    k_gemm_f64<4><<<grid, kThreads, 0, s>>>(Y, mref(Z, ldz), m, n, nb, nb, C, ldc, 0, 1);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
 }

@@ -9,9 +9,9 @@
 // narrow (about 2 DFMA/clk/SM) and every Householder step is a chain of
 // dependent FP64 operations and block barriers, so the design minimises the
 // number of sequential steps on the critical path:
-//  * leaves of ~64 rows, one CTA each: b Householder steps, then the leaf's
-//    compact-WY T (LAPACK dlarft from the Gram matrix V^T V, an independent
-//    recurrence per row of T);
+//  * leaves of at most leaf_rows rows, one CTA each: b Householder steps in
+//    the column-owner schedule below, which also yields the leaf's
+//    compact-WY T (T^-1 from the Gram matrix V^T V);
 //  * a fan-in-4 tree (last arriver combines, no waiting): the node stacks up
 //    to four R factors and runs b Householder steps on the stacked matrix (the
 //    zeros below the children's diagonals stay zero); with V = [I; V_2..V_4]
@@ -71,90 +71,252 @@ __device__ __forceinline__ double nr_rsqrt(double q) {
   return y;
 }
 
-// One Householder step on the column-major shared matrix S (ld): head row j,
-// tail rows {r < nrows : tail(r, j)}, columns j..ncols-1 (ncols <= 32).
-// beta = -sign(alpha) sqrt(q), q = alpha^2 + ||x||^2:  with r = q^-1/2,
-// beta = -sign(alpha) q r, 1/beta = -sign(alpha) r, tau = 1 - alpha / beta,
-// scal = 1 / (alpha - beta) (LAPACK dlarfg).  An all-zero tail takes the
-// reconstruction's convention tau = 2 (H = I - 2 e_j e_j^T, beta = -alpha)
-// rather than LAPACK's tau = 0, so that T^-1 = striu(V^T V) + diag(V^T V)/2
-// holds for every reflector.
-// Phase A (all warps): each thread owns rows and forms x_r S[r, c] for the 32
-// columns; a warp transpose-reduction (16+8+4+2+1 exchanges) leaves the sum
-// of column l in lane l.  Phase B (warp 0): column sums, scalars, head row.
-// Phase C: row owners update their tail rows and store v.  Three barriers.
-// part: 8 x 32 doubles, wsm: 32 doubles of shared scratch.
-template <class Tail>
-__device__ void h4_step(double* S, int ld, int nrows, int j, int ncols, Tail tail, double* tau,
-                        double* part, double* wsm) {
-  __shared__ double s_tau, s_scal;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nwarp_rows = (nrows + 31) >> 5;
-  if (warp < nwarp_rows) {
-    double p[32];
+// ---- Householder QR of a shared-memory block, column-owner schedule.
+//
+// The block S (column-major, ld rows, b <= 32 columns) is worked by 4 warps;
+// warp w owns the columns c with c % 4 == w for every row, and lane l owns the
+// rows l + 32 t.  Step j applies reflector j (vector v_j: 1 at the head row j,
+// S[j][r] on the tail rows) to every other column and computes reflector j+1:
+//  * the owner of column j+1 updates that column first, then forms reflector
+//    j+1 from it with warp-only reductions (nothing else waits for it but the
+//    next step);
+//  * every warp forms d_c = v_j^T S[c] for its other columns (one transposed
+//    warp reduction for all of them), updates the columns c > j and records
+//    d_c = v_c^T v_j for c < j: these are the strictly upper entries of
+//    T^-1 = striu(V^T V) + diag(V^T V) / 2 (the identity of the reference's
+//    compute_invT_from_Y, alg/QR/qr_2d/qr_2d.cxx:22-60), so T costs no extra
+//    pass over the rows;
+//  * one block barrier per step.
+// On GB300 every warp-wide FP64 instruction holds its SMSP's FP64 pipe for 64
+// cycles, so the schedule keeps one warp per SMSP and the per-step chain of
+// the owner short.  The reflector follows LAPACK dlarfg: beta = -sign(alpha)
+// sqrt(alpha^2 + |x|^2), tau = 1 - alpha / beta, v = x / (alpha - beta); an
+// all-zero tail takes tau = 2, beta = -alpha (a sign flip), the convention of
+// the reconstruction, so that the T^-1 identity holds for every reflector.
+constexpr int kLeafThreads = 128;   // 4 warps, one per SMSP
+constexpr int kMaxR = 8;            // rows per lane: leaves of up to 256 rows, nodes of 4 x 32
+
+// Sum over the warp of eight values per lane; every lane receives all eight sums.
+__device__ __forceinline__ void warp_sum8(const double (&d)[8], double (&out)[8]) {
+  const int lane = threadIdx.x & 31;
+  const bool u16 = (lane & 16) != 0, u8 = (lane & 8) != 0, u4 = (lane & 4) != 0;
+  double p[4], q[2];
 #pragma unroll
-    for (int c = 0; c < 32; ++c) p[c] = 0.0;
-    for (int r = tid; r < nrows; r += blockDim.x) {
-      if (!tail(r, j)) continue;
-      const double x = S[j * ld + r];
+  for (int k = 0; k < 4; ++k)
+    p[k] = (u16 ? d[k + 4] : d[k]) + __shfl_xor_sync(0xffffffffu, u16 ? d[k] : d[k + 4], 16);
 #pragma unroll
-      for (int c = 0; c < 32; ++c)
-        if (c >= j && c < ncols) p[c] = fma(x, S[c * ld + r], p[c]);
+  for (int k = 0; k < 2; ++k)
+    q[k] = (u8 ? p[k + 2] : p[k]) + __shfl_xor_sync(0xffffffffu, u8 ? p[k] : p[k + 2], 8);
+  double s = (u4 ? q[1] : q[0]) + __shfl_xor_sync(0xffffffffu, u4 ? q[0] : q[1], 4);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  // lane l now holds sum number 4 (l & 16 != 0) + 2 (l & 8 != 0) + (l & 4 != 0)
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    out[k] = __shfl_sync(0xffffffffu, s, (((k >> 2) & 1) << 4) | (((k >> 1) & 1) << 3) | ((k & 1) << 2));
+}
+
+// Reflector j from column j of S, by one warp: alpha = S[j][j], x = the tail
+// rows (lane l owns rows l + 32 t).  Writes beta to S[j][j],
+// v = x / (alpha - beta) to the tail rows, tau to s_tau[j] and v^T v / 2
+// (with the unit head) to g[j][j] (ld b).
+template <int R, class Tail>
+__device__ void h5_reflector(double* S, int ld, int rows, int j, int b, Tail tail, double* s_tau,
+                             double* g) {
+  const int lane = threadIdx.x & 31;
+  double* col = S + (size_t)j * ld;
+  double x[R];
+  double xn2 = 0.0;
+#pragma unroll
+  for (int t = 0; t < R; ++t) {
+    const int r = lane + 32 * t;
+    x[t] = (r < rows && tail(r, j)) ? col[r] : 0.0;
+    xn2 = fma(x[t], x[t], xn2);
+  }
+  xn2 = warp_sum(xn2);
+  const double alpha = col[j];
+  double tj, sc, beta;
+  if (xn2 == 0.0) {
+    tj = 2.0;
+    sc = 0.0;
+    beta = -alpha;
+  } else {
+    const double q = fma(alpha, alpha, xn2);
+    const double rq = nr_rsqrt(q);
+    const double sg = alpha >= 0.0 ? -1.0 : 1.0;   // -sign(alpha), sign(0) = +
+    beta = sg * q * rq;
+    tj = fma(-alpha, sg * rq, 1.0);
+    sc = nr_rcp(alpha - beta);
+  }
+#pragma unroll
+  for (int t = 0; t < R; ++t) {
+    const int r = lane + 32 * t;
+    if (r < rows && tail(r, j)) col[r] = x[t] * sc;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    col[j] = beta;
+    s_tau[j] = tj;
+    g[j * b + j] = 0.5 * fma(sc * sc, xn2, 1.0);
+  }
+}
+
+// Householder QR of S (rows x b, ld >= 32 R, R = ceil(rows / 32) rows per
+// lane); all kLeafThreads threads call it.  Afterwards S holds R (upper
+// triangle) and the reflector tails, s_tau the taus and g (b x b, ld b,
+// zeroed by the caller) T^-1.
+// Step j: warp (j+1) % 4 is the critical warp: it applies reflector j to
+// column j+1 and forms reflector j+1, and does nothing else, because a warp's
+// dependent FP64 chain occupies its SMSP's FP64 pipe.  The other three warps
+// share every other column c: d_c = v_j^T S[c] (a transposed reduction per 8
+// columns), then S[c] -= tau_j v_j d_c for c > j+1, or T^-1[c][j] = d_c for
+// c < j.  After the last reflector all four warps share the work.  The
+// updates load all of a group's rows before the first store, so that
+// independent columns are not serialised through shared memory.
+template <int R, class Tail>
+__device__ void h5_factor(double* S, int ld, int rows, int b, Tail tail, double* s_tau, double* g) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp == 0) h5_reflector<R>(S, ld, rows, 0, b, tail, s_tau, g);
+  __syncthreads();
+  for (int j = 0; j < b; ++j) {
+    const double* vj = S + (size_t)j * ld;
+    double vv[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) {
+      const int r = lane + 32 * t;
+      double v = 0.0;
+      if (r == j) v = 1.0;
+      else if (r < rows && tail(r, j)) v = vj[r];
+      vv[t] = v;
     }
+    const double tj = s_tau[j];
+    const int nxt = j + 1;
+    const bool has_crit = nxt < b;
+    const int crit = nxt & 3;
+    if (has_crit && warp == crit) {
+      // the next pivot column: apply reflector j, then form reflector j+1
+      double* cn = S + (size_t)nxt * ld;
+      double x[R];
+      double d = 0.0;
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) {
-      const bool up = (lane & off) != 0;
+      for (int t = 0; t < R; ++t) {
+        x[t] = cn[lane + 32 * t];
+        d = fma(vv[t], x[t], d);
+      }
+      d = warp_sum(d) * tj;
 #pragma unroll
-      for (int k = 0; k < off; ++k) {
-        const double send = up ? p[k] : p[k + off];
-        const double keep = up ? p[k + off] : p[k];
-        p[k] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+      for (int t = 0; t < R; ++t) cn[lane + 32 * t] = fma(-vv[t], d, x[t]);
+      __syncwarp();
+      h5_reflector<R>(S, ld, rows, nxt, b, tail, s_tau, g);
+    } else {
+      // bulk: this warp's share q of the columns other than j and j+1
+      const int nq = has_crit ? 3 : 4;
+      const int q = has_crit ? ((warp - crit + 3) & 3) : warp;   // 0 .. nq-1
+      for (int base = q; base < b; base += 8 * nq) {
+        double dd[8], D[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          dd[k] = 0.0;
+          const int c = base + k * nq;
+          if (c < b && c != j && c != nxt) {
+            const double* sc = S + (size_t)c * ld;
+#pragma unroll
+            for (int t = 0; t < R; ++t) dd[k] = fma(vv[t], sc[lane + 32 * t], dd[k]);
+          }
+        }
+        warp_sum8(dd, D);
+        // T^-1 entries for the columns before j
+        if (lane == 0) {
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const int c = base + k * nq;
+            if (c < j) g[j * b + c] = D[k];   // (V^T V)[c][j]
+          }
+        }
+        // updates of the columns after j+1, four columns per load group
+#pragma unroll
+        for (int h = 0; h < 8; h += 4) {
+          double xs[4][R];
+          bool act[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int c = base + (h + k) * nq;
+            act[k] = c < b && c > nxt;
+            if (act[k]) {
+              const double* sc = S + (size_t)c * ld;
+#pragma unroll
+              for (int t = 0; t < R; ++t) xs[k][t] = sc[lane + 32 * t];
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            if (!act[k]) continue;
+            const double dk = D[h + k] * tj;
+            double* sc = S + (size_t)(base + (h + k) * nq) * ld;
+#pragma unroll
+            for (int t = 0; t < R; ++t) sc[lane + 32 * t] = fma(-vv[t], dk, xs[k][t]);
+          }
+        }
       }
     }
-    part[warp * 32 + lane] = p[0];   // sum over this warp's rows of column `lane`
+    __syncthreads();
   }
-  __syncthreads();
-  if (warp == 0) {
-    double s = 0.0;
-    const int nw = nwarp_rows < 8 ? nwarp_rows : 8;
-    for (int w = 0; w < nw; ++w) s += part[w * 32 + lane];
-    const double xn2 = __shfl_sync(0xffffffffu, s, j);
-    const double alpha = S[j * ld + j];
-    double tj, sc, beta;
-    if (xn2 == 0.0) {
-      tj = 2.0;
-      sc = 0.0;
-      beta = -alpha;
-    } else {
-      const double q = fma(alpha, alpha, xn2);
-      const double r = nr_rsqrt(q);
-      const double sg = alpha >= 0.0 ? -1.0 : 1.0;   // -sign(alpha), sign(0) = +
-      beta = sg * q * r;
-      tj = fma(-alpha, sg * r, 1.0);
-      sc = nr_rcp(alpha - beta);
+}
+
+// Structure of an operand of h5_mm, on op(X): entries outside it read as 0
+// (and the unit diagonals as 1).
+enum : int { kSDense = 0, kSUpper = 1, kSUnitUpper = 2, kSUnitLower = 3 };
+
+__device__ __forceinline__ double h5_at(const double* X, int ld, bool tr, int st, int i, int k) {
+  if ((st == kSUpper || st == kSUnitUpper) && k < i) return 0.0;
+  if (st == kSUnitLower && k > i) return 0.0;
+  if ((st == kSUnitUpper || st == kSUnitLower) && k == i) return 1.0;
+  return tr ? X[i * ld + k] : X[k * ld + i];
+}
+
+// C = C0 + alpha op(A) op(B) for b x b shared-memory matrices (b <= 32; C0
+// may be nullptr, or C itself; C must not alias A or B).
+// The 32 x 32 output is cut into 8 x 8 tiles, each owned by one warp (lane l:
+// row l % 8, columns l / 8 and l / 8 + 4), and a tile's k loop only covers
+// the structural nonzeros of its row and column blocks (empty for the zero
+// tiles of a product of two upper-triangular operands), and the tiles are
+// dealt to the warps in order of decreasing work.  A warp-wide FP64 instruction is the unit of cost on this
+// GPU (about 4 per 77 cycles per SM), so this bounds the product by the
+// nonzero tile work instead of by the longest k range of any lane.
+__device__ void h5_mm(const double* A, int lda, bool at, int as, const double* B, int ldb, bool bt,
+                      int bs, double* C, int ldc, int b, double alpha, const double* C0) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int nt = (b + 7) >> 3;
+  // tiles in order of decreasing k extent: the diagonal distance d = tj - ti
+  // runs from nt - 1 down to -(nt - 1); tile number p walks that order
+  int p = 0;
+  for (int d = nt - 1; d >= -(nt - 1); --d) {
+    for (int ti = 0; ti < nt; ++ti) {
+      const int tj = ti + d;
+      if (tj < 0 || tj >= nt) continue;
+      const int i0 = ti * 8, j0 = tj * 8;
+      // k range of the tile from the operands' structure
+      int klo = 0, khi = b - 1;
+      if (as == kSUpper || as == kSUnitUpper) klo = i0;
+      if (as == kSUnitLower) khi = khi < i0 + 7 ? khi : i0 + 7;
+      if (bs == kSUpper || bs == kSUnitUpper) khi = khi < j0 + 7 ? khi : j0 + 7;
+      if (bs == kSUnitLower) klo = klo > j0 ? klo : j0;
+      // (an empty range still writes C = C0, or zero)
+      if ((p++ % nwarp) != warp) continue;
+      const int i = i0 + (lane & 7), jA = j0 + (lane >> 3), jB = jA + 4;
+      double acc0 = 0.0, acc1 = 0.0;
+      for (int k = klo; k <= khi; ++k) {
+        const double a = (i < b) ? h5_at(A, lda, at, as, i, k) : 0.0;
+        const double b0 = (jA < b) ? h5_at(B, ldb, bt, bs, k, jA) : 0.0;
+        const double b1 = (jB < b) ? h5_at(B, ldb, bt, bs, k, jB) : 0.0;
+        acc0 = fma(a, b0, acc0);
+        acc1 = fma(a, b1, acc1);
+      }
+      if (i < b) {
+        if (jA < b) C[jA * ldc + i] = fma(alpha, acc0, C0 ? C0[jA * ldc + i] : 0.0);
+        if (jB < b) C[jB * ldc + i] = fma(alpha, acc1, C0 ? C0[jB * ldc + i] : 0.0);
+      }
     }
-    // head row: w_c = S[j,c] + scal * s_c;  S[j,c] -= tau * w_c
-    if (lane > j && lane < ncols) {
-      const double w = fma(sc, s, S[lane * ld + j]);
-      wsm[lane] = w;
-      S[lane * ld + j] -= tj * w;
-    }
-    if (lane == 0) {
-      S[j * ld + j] = beta;
-      tau[j] = tj;
-      s_tau = tj;
-      s_scal = sc;
-    }
-  }
-  __syncthreads();
-  const double tj = s_tau, sc = s_scal;
-  // tail rows: v_r = scal * x_r;  S[r,c] -= tau * v_r * w_c;  column j <- v
-  for (int r = tid; r < nrows; r += blockDim.x) {
-    if (!tail(r, j)) continue;
-    const double v = sc * S[j * ld + r];
-    const double tv = tj * v;
-    for (int c = j + 1; c < ncols; ++c) S[c * ld + r] = fma(-tv, wsm[c], S[c * ld + r]);
-    S[j * ld + r] = v;
   }
   __syncthreads();
 }
@@ -210,47 +372,6 @@ __device__ void h4_tri_inv(const double* X, int b, bool unit, double* Xi, double
   __syncthreads();
 }
 
-// Compact-WY T (b x b, ld b) of the reflectors whose vectors are
-// V(r, i) = vget(r, i) over rows [0, rows): with G = V^T V, T^-1 =
-// striu(G) + diag(G) / 2 (the identity the reference uses in
-// compute_invT_from_Y, alg/QR/qr_2d/qr_2d.cxx:22-60; it is the T that makes
-// I - V T V^T orthogonal for the computed V).  The Gram dots are split into
-// four partial sums to shorten their dependent chains.
-template <class VGet>
-__device__ void h4_larft(VGet vget, int rows, int b, double* G, double* T, double* scratch) {
-  for (int idx = threadIdx.x; idx < b * b; idx += blockDim.x) {
-    const int i = idx % b, j = idx / b;
-    double acc = 0.0;
-    if (i <= j) {
-      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-      int r = 0;
-      for (; r + 3 < rows; r += 4) {
-        a0 = fma(vget(r, i), vget(r, j), a0);
-        a1 = fma(vget(r + 1, i), vget(r + 1, j), a1);
-        a2 = fma(vget(r + 2, i), vget(r + 2, j), a2);
-        a3 = fma(vget(r + 3, i), vget(r + 3, j), a3);
-      }
-      for (; r < rows; ++r) a0 = fma(vget(r, i), vget(r, j), a0);
-      acc = (a0 + a1) + (a2 + a3);
-      if (i == j) acc *= 0.5;
-    }
-    G[j * b + i] = acc;
-  }
-  __syncthreads();
-  h4_tri_inv(G, b, false, T, scratch);
-}
-
-// C = A * B for b x b shared matrices (ld b), A and B upper triangular.
-__device__ void h4_mm_upper(const double* A, const double* B, double* C, int b) {
-  for (int idx = threadIdx.x; idx < b * b; idx += blockDim.x) {
-    const int i = idx % b, j = idx / b;
-    double acc = 0.0;
-    for (int k = i; k <= j; ++k) acc = fma(A[k * b + i], B[j * b + k], acc);
-    C[j * b + i] = (i <= j) ? acc : 0.0;
-  }
-  __syncthreads();
-}
-
 __device__ void h4_load(double* dst, const double* src, int b) {
   for (int idx = threadIdx.x; idx < b * b; idx += blockDim.x) dst[idx] = __ldcg(src + idx);
   __syncthreads();
@@ -273,6 +394,7 @@ struct Hr4Args {
   double* Uinv;     // scratch b x b
   int* status;
   int P;
+  int ldS;          // leading dimension of the shared block (>= 32 * ceil(leaf rows / 32), >= 128)
   int depth;
   int nlev[kMaxLevels + 1];
   int base[kMaxLevels + 1];
@@ -300,7 +422,7 @@ __device__ void h4_root(const Hr4Args& a, double* sm) {
   for (int lvl = a.depth; lvl >= 1; --lvl) {
     if (h4_children(a, lvl, 0) > 1) {
       h4_load(sX, a.Qn + ((size_t)a.base[lvl] * kFan + 0) * b * b, b);
-      h4_mm_upper(sX, sM, sQ, b);
+      h5_mm(sX, b, false, kSUpper, sM, b, false, kSUpper, sQ, b, b, 1.0, nullptr);
       for (int idx = tid; idx < b * b; idx += blockDim.x) sM[idx] = sQ[idx];
       __syncthreads();
     }
@@ -311,38 +433,22 @@ __device__ void h4_root(const Hr4Args& a, double* sm) {
     sY[idx] = (r > c) ? __ldcg(a.Vw + (int64_t)c * a.m + r) : (r == c ? 1.0 : 0.0);
   }
   h4_load(sT, a.Tl, b);
-  for (int idx = tid; idx < b * b; idx += blockDim.x) {     // sX = V0^T C0
-    const int i = idx % b, j = idx / b;
-    double acc = 0.0;
-    for (int k = i; k < b; ++k) acc = fma(sY[i * b + k], sM[j * b + k], acc);
-    sX[idx] = acc;
-  }
-  __syncthreads();
-  for (int idx = tid; idx < b * b; idx += blockDim.x) {     // sQ = T0 sX
-    const int i = idx % b, j = idx / b;
-    double acc = 0.0;
-    for (int k = i; k < b; ++k) acc = fma(sT[k * b + i], sX[j * b + k], acc);
-    sQ[idx] = acc;
-  }
-  __syncthreads();
-  for (int idx = tid; idx < b * b; idx += blockDim.x) {     // sX = C0 - V0 sQ
-    const int i = idx % b, j = idx / b;
-    double acc = sM[idx];
-    for (int k = 0; k <= i; ++k) acc = fma(-sY[k * b + i], sQ[j * b + k], acc);
-    sX[idx] = acc;
-  }
-  __syncthreads();
+  h5_mm(sY, b, true, kSUnitUpper, sM, b, false, kSUpper, sX, b, b, 1.0, nullptr);   // sX = V0^T C0
+  h5_mm(sT, b, false, kSUpper, sX, b, false, kSDense, sQ, b, b, 1.0, nullptr);      // sQ = T0 sX
+  h5_mm(sY, b, false, kSUnitLower, sQ, b, false, kSDense, sX, b, b, -1.0, sM);      // sX = C0 - V0 sQ
   double* sL = sX;   // Q1_top, becomes L\U
+  __shared__ double s_rpiv;
   for (int i = 0; i < b; ++i) {
     if (tid == 0) {
       const double d = sL[i * b + i];
       const int s = d > 0.0 ? -1 : 1;
       s_sign[i] = s;
       sL[i * b + i] = d - (double)s;
+      s_rpiv = nr_rcp(d - (double)s);   // |d - s| >= 1: the sign choice keeps the pivot away from 0
     }
     __syncthreads();
-    const double piv = sL[i * b + i];
-    for (int r = i + 1 + tid; r < b; r += blockDim.x) sL[i * b + r] /= piv;
+    const double rpiv = s_rpiv;
+    for (int r = i + 1 + tid; r < b; r += blockDim.x) sL[i * b + r] *= rpiv;
     __syncthreads();
     const int n = b - i - 1;
     for (int idx = tid; idx < n * n; idx += blockDim.x) {
@@ -365,7 +471,7 @@ __device__ void h4_root(const Hr4Args& a, double* sm) {
   }
   __syncthreads();
   h4_tri_inv(sY, b, true, sM, scratch);
-  h4_mm_upper(sQ, sM, sT, b);
+  h5_mm(sQ, b, false, kSUpper, sM, b, false, kSUpper, sT, b, b, 1.0, nullptr);
   for (int idx = tid; idx < b * b; idx += blockDim.x) {
     const int r = idx % b, c = idx / b;
     a.T[c * a.ldT + r] = (r <= c) ? -sT[c * b + r] : 0.0;
@@ -381,36 +487,44 @@ __device__ void h4_root(const Hr4Args& a, double* sm) {
   if (bad) atomicExch(a.status, CANDMC_ERR_NUMERIC);
 }
 
-__global__ void __launch_bounds__(kThreads) k_hr4_leaf_tree(Hr4Args a) {
+__global__ void __launch_bounds__(kLeafThreads) k_hr4_leaf_tree(Hr4Args a) {
   extern __shared__ double sm4[];
   __shared__ double s_tau[kDirectB];
-  __shared__ double s_part[8 * 32];
-  __shared__ double s_w[32];
   __shared__ int s_last;
   const int b = a.b, tid = threadIdx.x;
   const int leaf = blockIdx.x;
   const int64_t r0 = t4_leaf_row0(a.m, a.P, leaf);
   const int L = (int)(t4_leaf_row0(a.m, a.P, leaf + 1) - r0);
+  const int ldS = a.ldS;
   double* S = sm4;
-  double* G = sm4 + (size_t)(L > kFan * b ? L : kFan * b) * b;
+  double* G = S + (size_t)ldS * b;
   double* Tt = G + b * b;
   double* scratch = Tt + b * b;
 
-  // ---- leaf: Householder QR, R, V and T out
+  // ---- leaf: Householder QR of rows [r0, r0 + L); rows L..ldS-1 are zero
   for (int c = 0; c < b; ++c)
-    for (int r = tid; r < L; r += blockDim.x) S[c * L + r] = a.A[c * a.lda + r0 + r];
+    for (int r = tid; r < ldS; r += blockDim.x) S[c * ldS + r] = (r < L) ? a.A[c * a.lda + r0 + r] : 0.0;
+  for (int idx = tid; idx < b * b; idx += blockDim.x) G[idx] = 0.0;
   __syncthreads();
-  for (int j = 0; j < b; ++j)
-    h4_step(S, L, L, j, b, [](int r, int jj) { return r > jj; }, s_tau, s_part, s_w);
+  {
+    auto tail = [](int r, int j) { return r > j; };
+    switch ((L + 31) >> 5) {
+      case 1: h5_factor<1>(S, ldS, L, b, tail, s_tau, G); break;
+      case 2: h5_factor<2>(S, ldS, L, b, tail, s_tau, G); break;
+      case 3: h5_factor<3>(S, ldS, L, b, tail, s_tau, G); break;
+      case 4: h5_factor<4>(S, ldS, L, b, tail, s_tau, G); break;
+      default: h5_factor<8>(S, ldS, L, b, tail, s_tau, G); break;
+    }
+  }
   double* Rl = a.Rn + (size_t)(a.base[0] + leaf) * b * b;
   for (int idx = tid; idx < b * b; idx += blockDim.x) {
     const int r = idx % b, c = idx / b;
-    Rl[idx] = (r <= c) ? S[c * L + r] : 0.0;
+    Rl[idx] = (r <= c) ? S[c * ldS + r] : 0.0;
   }
   for (int c = 0; c < b; ++c)
-    for (int r = tid; r < L; r += blockDim.x) a.Vw[(int64_t)c * a.m + r0 + r] = (r > c) ? S[c * L + r] : 0.0;
-  h4_larft([&](int r, int i) { return r > i ? S[i * L + r] : (r == i ? 1.0 : 0.0); }, L, b, G, Tt,
-           scratch);
+    for (int r = tid; r < L; r += blockDim.x)
+      a.Vw[(int64_t)c * a.m + r0 + r] = (r > c) ? S[c * ldS + r] : 0.0;
+  h4_tri_inv(G, b, false, Tt, scratch);
   double* Tleaf = a.Tl + (size_t)leaf * b * b;
   for (int idx = tid; idx < b * b; idx += blockDim.x) Tleaf[idx] = Tt[idx];
 
@@ -434,56 +548,39 @@ __global__ void __launch_bounds__(kThreads) k_hr4_leaf_tree(Hr4Args a) {
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    // stack the children's R factors: rows [k b, k b + b) hold child k (ld = nch * b)
-    const int ld2 = nch * b;
-    for (int k = 0; k < nch; ++k) {
-      const double* Rk = a.Rn + (size_t)(a.base[lvl] + parent * kFan + k) * b * b;
-      for (int idx = tid; idx < b * b; idx += blockDim.x) {
-        const int r = idx % b, c = idx / b;
-        S[c * ld2 + k * b + r] = (r <= c) ? __ldcg(Rk + idx) : 0.0;
+    // stack the children's R factors: child k occupies rows [32 k, 32 k + b)
+    // (rows b..31 of every child stay zero)
+    const int rows = nch * 32;
+    for (int c = 0; c < b; ++c)
+      for (int r = tid; r < rows; r += blockDim.x) {
+        const int k = r >> 5, i = r & 31;
+        const double* Rk = a.Rn + (size_t)(a.base[lvl] + parent * kFan + k) * b * b;
+        S[c * ldS + r] = (i <= c) ? __ldcg(Rk + c * b + i) : 0.0;
       }
-    }
+    for (int idx = tid; idx < b * b; idx += blockDim.x) G[idx] = 0.0;
     __syncthreads();
-    // reflector j: head row j, tail = rows 0..j of every other child (the
-    // children are upper triangular, so nothing below their diagonals is touched)
-    const int bb = b;
-    for (int j = 0; j < b; ++j)
-      h4_step(S, ld2, ld2, j, b, [bb](int r, int jj) { return r >= bb && (r % bb) <= jj; }, s_tau,
-              s_part, s_w);
+    // reflector j: head row j (child 0), tail = rows 0..j of every other child
+    // (the children are upper triangular, so nothing below their diagonals is touched)
+    // (rows 32 k .. 32 k + j of children k >= 1 form the tail of reflector j)
+    h5_factor<4>(S, ldS, rows, b, [](int r, int j) { return r >= 32 && (r & 31) <= j; }, s_tau, G);
     for (int idx = tid; idx < b * b; idx += blockDim.x) {
       const int r = idx % b, c = idx / b;
-      Rpar[idx] = (r <= c) ? S[c * ld2 + r] : 0.0;
+      Rpar[idx] = (r <= c) ? S[c * ldS + r] : 0.0;
     }
-    // V = [I; V_1; ..; V_{nch-1}], V_k upper triangular: G = I + sum_k V_k^T V_k,
-    // with the diagonal halved, is T^-1
-    for (int idx = tid; idx < b * b; idx += blockDim.x) {
-      const int i = idx % b, j = idx / b;
-      double acc = 0.0;
-      if (i <= j) {
-        acc = (i == j) ? 1.0 : 0.0;
-        for (int k = 1; k < nch; ++k)
-          for (int r = 0; r <= i; ++r) acc = fma(S[i * ld2 + k * b + r], S[j * ld2 + k * b + r], acc);
-        if (i == j) acc *= 0.5;
-      }
-      G[j * b + i] = acc;
-    }
-    __syncthreads();
     h4_tri_inv(G, b, false, Tt, scratch);
     double* Qp = a.Qn + (size_t)(a.base[lvl + 1] + parent) * kFan * b * b;
-    // Q_1 = I - T;  Q_k = -V_k T  (V_k = rows [k b, k b + b) of the tail, upper triangular)
+    // V = [I; V_1; ..; V_{nch-1}] (V_k upper triangular):
+    // Q_1 = I - T;  Q_k = -V_k T
     for (int idx = tid; idx < b * b; idx += blockDim.x) {
       const int r = idx % b, c = idx / b;
       Qp[idx] = ((r == c) ? 1.0 : 0.0) - ((r <= c) ? Tt[c * b + r] : 0.0);
     }
     for (int k = 1; k < nch; ++k) {
-      for (int idx = tid; idx < b * b; idx += blockDim.x) {
-        const int r = idx % b, c = idx / b;
-        double acc = 0.0;
-        for (int kk = r; kk <= c; ++kk) acc = fma(S[kk * ld2 + k * b + r], Tt[c * b + kk], acc);
-        Qp[(size_t)k * b * b + idx] = (r <= c) ? -acc : 0.0;
-      }
+      double* Qk = G;   // G is free once T is formed
+      h5_mm(S + 32 * k, ldS, false, kSUpper, Tt, b, false, kSUpper, Qk, b, b, -1.0, nullptr);
+      for (int idx = tid; idx < b * b; idx += blockDim.x) Qp[(size_t)k * b * b + idx] = Qk[idx];
+      __syncthreads();
     }
-    __syncthreads();
     node = parent;
   }
   __threadfence();
@@ -510,7 +607,7 @@ __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
     if (h4_children(a, lvl, nd) > 1) {
       const int k = child - nd * kFan;
       h4_load(sX, a.Qn + ((size_t)(a.base[lvl] + nd) * kFan + k) * b * b, b);
-      h4_mm_upper(sX, sM, sY, b);
+      h5_mm(sX, b, false, kSUpper, sM, b, false, kSUpper, sY, b, b, 1.0, nullptr);
       for (int idx = tid; idx < b * b; idx += blockDim.x) sM[idx] = sY[idx];
       __syncthreads();
     }
@@ -521,20 +618,8 @@ __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
     sY[idx] = (r > c) ? a.Vw[(int64_t)c * a.m + r0 + r] : (r == c ? 1.0 : 0.0);
   }
   h4_load(sT, a.Tl + (size_t)leaf * b * b, b);
-  for (int idx = tid; idx < b * b; idx += blockDim.x) {
-    const int i = idx % b, j = idx / b;
-    double acc = 0.0;
-    for (int k = i; k < b; ++k) acc = fma(sY[i * b + k], sM[j * b + k], acc);
-    sX[idx] = acc;
-  }
-  __syncthreads();
-  for (int idx = tid; idx < b * b; idx += blockDim.x) {
-    const int i = idx % b, j = idx / b;
-    double acc = 0.0;
-    for (int k = i; k < b; ++k) acc = fma(sT[k * b + i], sX[j * b + k], acc);
-    sY[idx] = acc;   // sY now holds Z (V_top no longer needed)
-  }
-  __syncthreads();
+  h5_mm(sY, b, true, kSUnitUpper, sM, b, false, kSUpper, sX, b, b, 1.0, nullptr);   // sX = V_top^T M
+  h5_mm(sT, b, false, kSUpper, sX, b, false, kSDense, sY, b, b, 1.0, nullptr);      // sY = Z = T sX
   for (int64_t r = r0 + tid; r < r1; r += blockDim.x) {
     if (r < b) continue;
     const int rl = (int)(r - r0);
@@ -556,7 +641,8 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
                int64_t ldW, int* d_status, cudaStream_t s) {
   if (b < 1 || b > kDirectB || m < b) return CANDMC_ERR_ARG;
   const int64_t leaf_rows = std::max<int64_t>(32, std::min<int64_t>(g_leaf_rows, 256));
-  int64_t P = std::max<int64_t>(1, std::min<int64_t>(m / leaf_rows, m / b));
+  // leaves of at most leaf_rows rows and at least b rows
+  int64_t P = std::max<int64_t>(1, std::min<int64_t>((m + leaf_rows - 1) / leaf_rows, m / b));
   if (P > (1 << 24)) return CANDMC_ERR_ARG;
   Hr4Args a{};
   a.P = (int)P;
@@ -573,10 +659,15 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   const int nnodes = total;
   const int64_t Lmax = (m + P - 1) / P;
   const size_t nb2 = (size_t)b * b;
-  // leaf/node matrix + G + T + tri-inverse workspace; the root reuses the
-  // front of the same area for six b x b buffers plus the workspace
-  const size_t sm = sizeof(double) * ((size_t)std::max<int64_t>(Lmax, kFan * b) * b + 6 * nb2 +
-                                      kTriScratch);
+  // shared block: rows padded to whole warps of lanes, at least the 4 x 32
+  // rows of a tree node
+  const int64_t ldS = std::max<int64_t>((Lmax + 31) / 32 * 32, kFan * 32);
+  if (ldS > 32 * kMaxR) return CANDMC_ERR_ARG;
+  a.ldS = (int)ldS;
+  // block + G + T + tri-inverse workspace; the root reuses the front of the
+  // same area for six b x b buffers plus the workspace
+  const size_t sm = sizeof(double) * std::max<size_t>((size_t)ldS * b + 2 * nb2 + kTriScratch,
+                                                      6 * nb2 + kTriScratch);
   if (sm > 200 * 1024) return CANDMC_ERR_ARG;
   DevBuf vw, tl, rn, qn, cnt, uinv;
   CANDMC_RET(vw.alloc(sizeof(double) * (size_t)m * b, s));
@@ -598,7 +689,7 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   }
   {
     ProfScope ps(CANDMC_KCLASS_PANEL_LEAF, 2.0 * m * b * b, s);
-    k_hr4_leaf_tree<<<(unsigned)P, kThreads, sm, s>>>(a);
+    k_hr4_leaf_tree<<<(unsigned)P, kLeafThreads, sm, s>>>(a);
   }
   CANDMC_CK(cudaGetLastError());
   {
