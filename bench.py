@@ -574,7 +574,7 @@ def wl_tsqr_hr(args, ctx):
     f = qr_flops(m, b)
     value = ctx.world * f * args.steps / (t_max / 1e3) / 1e9
     roof = fp64_roof(prof, ["panel_leaf", "panel_y"],
-                     "k_hr4_leaf_tree + k_hr4_form_y (TSQR leaves, fan-in-4 tree, reconstruction, Y)",
+                     "k_hr6_pipe (pipelined TSQR tree) or k_hr4_leaf_tree, + k_hr4_form_y (reconstruction, Y)",
                      t_max)
     hbm = measured_peaks().get("hbm_gbs", 6778.0)
     bytes_alg = 16.0 * m * b
@@ -774,7 +774,7 @@ def wl_batched(args, ctx):
     solves = ctx.world * count * args.steps / (t_max / 1e3)
     f = sum(qr_flops(m, n) for m, n in sizes)
     by = sum(16.0 * m * n for m, n in sizes)
-    roof = fp64_roof(prof, ["panel_leaf", "panel_y"], "k_hr4_leaf_tree + k_hr4_form_y", t_max)
+    roof = fp64_roof(prof, ["panel_leaf", "panel_y"], "k_hr6_pipe / k_hr4_leaf_tree + k_hr4_form_y", t_max)
     hbm = measured_peaks().get("hbm_gbs", 6778.0)
     roof["step_fp64_tflops"] = f * args.steps / (t_max / 1e3) / 1e12
     roof["hbm"] = {"achieved_gbs": by * args.steps / (t_max / 1e3) / 1e9, "peak_gbs": hbm,

@@ -133,6 +133,11 @@ extern "C" int candmc_set_tuning(const char* key, int64_t value) {
     g_leaf_rows = value;
     return CANDMC_OK;
   }
+  if (std::string(key) == "pipe_tree") {
+    if (value != 0 && value != 1) return set_error(CANDMC_ERR_ARG, "pipe_tree is 0 or 1");
+    g_pipe_tree = (int)value;
+    return CANDMC_OK;
+  }
   return set_error(CANDMC_ERR_ARG, "unknown tuning key");
 }
 
@@ -148,10 +153,11 @@ extern "C" int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t*
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!use_graph) return batched_issue(nprob, m, n, A, lda, B, nstreams, s);
   std::vector<int64_t> key;
-  key.reserve(6 * nprob + 3);
+  key.reserve(6 * nprob + 4);
   key.push_back(nprob);
   key.push_back(nstreams);
   key.push_back(g_leaf_rows);
+  key.push_back(g_pipe_tree);
   for (int64_t i = 0; i < nprob; ++i) {
     key.push_back(m[i]);
     key.push_back(n[i]);

@@ -31,6 +31,7 @@ int hr_direct(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, 
               int64_t ldW, int* d_status, cudaStream_t s);
 // tsqr4.cu: direct TSQR-HR with a fan-in-4 tree and compact-WY Q blocks.
 extern int64_t g_leaf_rows;
+extern int g_pipe_tree;
 int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
                int64_t ldW, int* d_status, cudaStream_t s);
 

@@ -36,6 +36,8 @@ constexpr int kFan = 4;
 
 // Target rows per TSQR leaf (tuning knob, candmc_set_tuning("leaf_rows", v)).
 int64_t g_leaf_rows = 64;
+// Pipelined tree on/off (tuning knob, candmc_set_tuning("pipe_tree", 0|1)).
+int g_pipe_tree = 1;
 constexpr int kTriScratch = 512 + kDirectB * kDirectB;   // h4_tri_inv workspace (doubles)
 
 __device__ __forceinline__ int64_t t4_leaf_row0(int64_t m, int P, int i) {
@@ -173,12 +175,20 @@ __device__ void h5_reflector(double* S, int ld, int rows, int j, int b, Tail tai
 // c < j.  After the last reflector all four warps share the work.  The
 // updates load all of a group's rows before the first store, so that
 // independent columns are not serialised through shared memory.
-template <int R, class Tail>
-__device__ void h5_factor(double* S, int ld, int rows, int b, Tail tail, double* s_tau, double* g) {
+struct NoPublish {
+  __device__ void operator()(const double*, int, int) const {}
+};
+
+template <int R, class Tail, class Pub = NoPublish>
+__device__ void h5_factor(double* S, int ld, int rows, int b, Tail tail, double* s_tau, double* g,
+                          Pub pub = Pub()) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (warp == 0) h5_reflector<R>(S, ld, rows, 0, b, tail, s_tau, g);
   __syncthreads();
   for (int j = 0; j < b; ++j) {
+    // column j of R is final now (its last update was step j-1): a warp
+    // other than this step's critical one may publish it
+    if (warp == ((j + 2) & 3)) pub(S, ld, j);
     const double* vj = S + (size_t)j * ld;
     double vv[R];
 #pragma unroll
@@ -393,6 +403,10 @@ struct Hr4Args {
   int64_t ldW;
   double* Uinv;     // scratch b x b
   int* status;
+  unsigned* prog;   // pipelined tree: columns of R published by each node
+  unsigned* done;   // pipelined tree: node finished (T, Q blocks, V written)
+  unsigned* ticket; // pipelined tree: role counter
+  int* fail;        // pipelined tree: a wait gave up
   int P;
   int ldS;          // leading dimension of the shared block (>= 32 * ceil(leaf rows / 32), >= 128)
   int depth;
@@ -588,6 +602,272 @@ __global__ void __launch_bounds__(kLeafThreads) k_hr4_leaf_tree(Hr4Args a) {
   h4_root(a, sm4);
 }
 
+// ---- pipelined tree: one launch for the leaves and every internal node.
+//
+// The levels of the tree above do not overlap: a node starts when its
+// children have finished all b columns, so a panel costs (1 + depth) b
+// sequential Householder steps.  Here a node starts column j as soon as its
+// children have published column j of their R: leaves run the right-looking
+// steps above and publish each column of R when it becomes final; internal
+// nodes run left-looking, applying their earlier reflectors to the arriving
+// column through the compact-WY factor T they build as they go (LAPACK
+// dlarft's column recurrence T[0:j, j] = -tau_j T[0:j, 0:j] V^T v_j), so the
+// panel costs about b + depth steps.  Roles come from an atomic ticket
+// (leaves first, then the nodes level by level), so a node only waits for
+// CTAs that took a lower ticket and are already running, whatever the
+// scheduling order.  Every wait is bounded: a wait that runs out records
+// CANDMC_ERR_TIMEOUT, and the CTA releases its own flags and returns, so no
+// other CTA is left waiting on it.
+constexpr long kSpinLimit = 1L << 22;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// One thread: wait until *p >= v.  False when the wait gave up or another CTA
+// of this launch did.
+__device__ bool h6_wait(const Hr4Args& a, const unsigned* p, unsigned v) {
+  for (long it = 0; it < kSpinLimit; ++it) {
+    if (ld_acquire(p) >= v) return true;
+    if (*(volatile int*)a.fail) return false;
+    __nanosleep(100);
+  }
+  atomicExch(a.fail, 1);
+  atomicExch(a.status, CANDMC_ERR_TIMEOUT);
+  return false;
+}
+
+__device__ void h6_release_all(const Hr4Args& a, int f) {
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release(a.prog + f, (unsigned)a.b);
+    st_release(a.done + f, 1u);
+  }
+}
+
+struct LeafPublish {
+  double* Rcol;
+  int b;
+  unsigned* prog;
+  __device__ void operator()(const double* S, int ld, int j) const {
+    const int lane = threadIdx.x & 31;
+    if (lane <= j) Rcol[j * b + lane] = S[j * ld + lane];
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) st_release(prog, (unsigned)(j + 1));
+  }
+};
+
+__device__ void h6_leaf(const Hr4Args& a, int leaf, double* sm, double* s_tau) {
+  const int b = a.b, tid = threadIdx.x;
+  const int64_t r0 = t4_leaf_row0(a.m, a.P, leaf);
+  const int L = (int)(t4_leaf_row0(a.m, a.P, leaf + 1) - r0);
+  const int ldS = a.ldS;
+  double* S = sm;
+  double* G = S + (size_t)ldS * b;
+  double* Tt = G + b * b;
+  double* scratch = Tt + b * b;
+  for (int c = 0; c < b; ++c)
+    for (int r = tid; r < ldS; r += blockDim.x) S[c * ldS + r] = (r < L) ? a.A[c * a.lda + r0 + r] : 0.0;
+  for (int idx = tid; idx < b * b; idx += blockDim.x) G[idx] = 0.0;
+  __syncthreads();
+  const LeafPublish pub{a.Rn + (size_t)leaf * b * b, b, a.prog + leaf};
+  auto tail = [](int r, int j) { return r > j; };
+  switch ((L + 31) >> 5) {
+    case 1: h5_factor<1>(S, ldS, L, b, tail, s_tau, G, pub); break;
+    case 2: h5_factor<2>(S, ldS, L, b, tail, s_tau, G, pub); break;
+    case 3: h5_factor<3>(S, ldS, L, b, tail, s_tau, G, pub); break;
+    case 4: h5_factor<4>(S, ldS, L, b, tail, s_tau, G, pub); break;
+    default: h5_factor<8>(S, ldS, L, b, tail, s_tau, G, pub); break;
+  }
+  for (int c = 0; c < b; ++c)
+    for (int r = tid; r < L; r += blockDim.x)
+      a.Vw[(int64_t)c * a.m + r0 + r] = (r > c) ? S[c * ldS + r] : 0.0;
+  h4_tri_inv(G, b, false, Tt, scratch);
+  double* Tleaf = a.Tl + (size_t)leaf * b * b;
+  for (int idx = tid; idx < b * b; idx += blockDim.x) Tleaf[idx] = Tt[idx];
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) st_release(a.done + leaf, 1u);
+}
+
+__device__ void h6_node(const Hr4Args& a, int f, double* sm, double* s_tau, int* s_ok) {
+  const int b = a.b, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int lvl = 1;
+  while (lvl < a.depth && f >= a.base[lvl + 1]) ++lvl;
+  const int idx = f - a.base[lvl];
+  const int nch = h4_children(a, lvl, idx);
+  const int child0 = a.base[lvl - 1] + idx * kFan;   // flat id of child 0
+  double* Rme = a.Rn + (size_t)f * b * b;
+  constexpr int ld = kFan * 32;   // child k at rows [32 k, 32 k + b)
+  double* S = sm;
+  double* Tn = S + ld * b;
+  double* Qk = Tn + b * b;
+  double* zv = Qk + b * b;
+  double* wv = zv + 32;
+  double* part = wv + 32;
+  for (int i = tid; i < ld * b; i += blockDim.x) S[i] = 0.0;
+  for (int i = tid; i < b * b; i += blockDim.x) Tn[i] = 0.0;
+  __syncthreads();
+  auto tail = [](int r, int j) { return r >= 32 && (r & 31) <= j; };
+  for (int j = 0; j < b; ++j) {
+    // (1) column j of every child
+    if (tid == 0) {
+      bool ok = true;
+      for (int k = 0; k < nch && ok; ++k) ok = h6_wait(a, a.prog + child0 + k, (unsigned)(j + 1));
+      *s_ok = ok;
+    }
+    __syncthreads();
+    if (!*s_ok) {
+      h6_release_all(a, f);
+      return;
+    }
+    if (nch == 1) {   // a pass-through node: its R is its child's
+      if (warp == 0) {
+        if (lane <= j) Rme[j * b + lane] = __ldcg(a.Rn + (size_t)child0 * b * b + j * b + lane);
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(a.prog + f, (unsigned)(j + 1));
+      }
+      continue;
+    }
+    // (2) stack the children's column j
+    if (warp < nch && lane <= j)
+      S[j * ld + 32 * warp + lane] = __ldcg(a.Rn + (size_t)(child0 + warp) * b * b + j * b + lane);
+    __syncthreads();
+    if (j > 0) {
+      // (3) z_p = v_p^T s_j for p < j: head row p plus the children's rows
+      double dd[8], D[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        dd[q] = 0.0;
+        const int pp = warp + 4 * q;
+        if (pp < j)
+          for (int k = 1; k < nch; ++k) dd[q] = fma(S[pp * ld + 32 * k + lane], S[j * ld + 32 * k + lane], dd[q]);
+      }
+      warp_sum8(dd, D);
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int pp = warp + 4 * q;
+          if (pp < j) zv[pp] = S[j * ld + pp] + D[q];
+        }
+      }
+      __syncthreads();
+      // (4) w = T^T z
+      {
+        double acc = 0.0;
+        if (lane < j)
+          for (int pp = warp; pp <= lane; pp += 4) acc = fma(Tn[lane * b + pp], zv[pp], acc);
+        part[warp * 32 + lane] = acc;
+      }
+      __syncthreads();
+      if (warp == 0 && lane < j) wv[lane] = (part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]);
+      __syncthreads();
+      // (5) s_j -= V w: head rows p < j and the children's rows i < j
+      if (warp == 0) {
+        if (lane < j) S[j * ld + lane] -= wv[lane];
+      } else if (warp < nch && lane < j) {
+        const int k = warp;
+        double acc = 0.0;
+        for (int pp = lane; pp < j; ++pp) acc = fma(S[pp * ld + 32 * k + lane], wv[pp], acc);
+        S[j * ld + 32 * k + lane] -= acc;
+      }
+      __syncthreads();
+    }
+    // (6) reflector j, then publish column j of R
+    if (warp == 0) {
+      h5_reflector<kFan>(S, ld, nch * 32, j, b, tail, s_tau, Qk);
+      __syncwarp();
+      if (lane <= j) Rme[j * b + lane] = S[j * ld + lane];
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) st_release(a.prog + f, (unsigned)(j + 1));
+    }
+    __syncthreads();
+    // (7) column j of T: T[p][j] = -tau_j sum_{q=p}^{j-1} T[p][q] (v_q^T v_j)
+    if (j > 0) {
+      double dd[8], D[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        dd[q] = 0.0;
+        const int pp = warp + 4 * q;
+        if (pp < j)
+          for (int k = 1; k < nch; ++k) dd[q] = fma(S[pp * ld + 32 * k + lane], S[j * ld + 32 * k + lane], dd[q]);
+      }
+      warp_sum8(dd, D);
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int pp = warp + 4 * q;
+          if (pp < j) zv[pp] = D[q];
+        }
+      }
+      __syncthreads();
+      {
+        double acc = 0.0;
+        if (lane < j)
+          for (int q = warp; q < j; q += 4)
+            if (q >= lane) acc = fma(Tn[q * b + lane], zv[q], acc);
+        part[warp * 32 + lane] = acc;
+      }
+      __syncthreads();
+      if (warp == 0 && lane < j)
+        Tn[j * b + lane] = -s_tau[j] * ((part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]));
+    }
+    if (tid == 0) Tn[j * b + j] = s_tau[j];
+    __syncthreads();
+  }
+  if (nch > 1) {
+    // Q blocks of the node: Q_1 = I - T;  Q_k = -V_k T
+    double* Qp = a.Qn + (size_t)f * kFan * b * b;
+    for (int i = tid; i < b * b; i += blockDim.x) {
+      const int r = i % b, c = i / b;
+      Qp[i] = ((r == c) ? 1.0 : 0.0) - ((r <= c) ? Tn[c * b + r] : 0.0);
+    }
+    for (int k = 1; k < nch; ++k) {
+      h5_mm(S + 32 * k, ld, false, kSUpper, Tn, b, false, kSUpper, Qk, b, b, -1.0, nullptr);
+      for (int i = tid; i < b * b; i += blockDim.x) Qp[(size_t)k * b * b + i] = Qk[i];
+      __syncthreads();
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) st_release(a.done + f, 1u);
+  if (lvl == a.depth) {
+    // the root: the chain of leaf 0 (its T and V, the Q_1 blocks of its
+    // ancestors) must be complete
+    if (tid == 0) {
+      bool ok = h6_wait(a, a.done + 0, 1u);
+      for (int l = 1; l < a.depth && ok; ++l) ok = h6_wait(a, a.done + a.base[l], 1u);
+      *s_ok = ok;
+    }
+    __syncthreads();
+    if (!*s_ok) return;
+    __threadfence();
+    h4_root(a, sm);
+  }
+}
+
+__global__ void __launch_bounds__(kLeafThreads) k_hr6_pipe(Hr4Args a) {
+  extern __shared__ double sm6[];
+  __shared__ double s_tau[kDirectB];
+  __shared__ int s_role, s_ok;
+  if (threadIdx.x == 0) s_role = (int)atomicAdd(a.ticket, 1u);
+  __syncthreads();
+  const int f = s_role;   // flat tree id: leaves 0 .. P-1, then the nodes level by level
+  if (f < a.P)
+    h6_leaf(a, f, sm6, s_tau);
+  else
+    h6_node(a, f, sm6, s_tau, &s_ok);
+}
+
 __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
   extern __shared__ double sm4[];
   const int b = a.b, tid = threadIdx.x;
@@ -669,27 +949,44 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   const size_t sm = sizeof(double) * std::max<size_t>((size_t)ldS * b + 2 * nb2 + kTriScratch,
                                                       6 * nb2 + kTriScratch);
   if (sm > 200 * 1024) return CANDMC_ERR_ARG;
+  // the pipelined tree while the whole tree is a modest number of CTAs (a
+  // latency-bound panel); the level-by-level tree for many leaves, where the
+  // leaves dominate and the pipeline would only add synchronisation
+  const bool pipe = a.depth >= 1 && g_pipe_tree && nnodes <= 4096;
   DevBuf vw, tl, rn, qn, cnt, uinv;
   CANDMC_RET(vw.alloc(sizeof(double) * (size_t)m * b, s));
   CANDMC_RET(tl.alloc(sizeof(double) * nb2 * P, s));
   CANDMC_RET(rn.alloc(sizeof(double) * nb2 * nnodes, s));
   CANDMC_RET(qn.alloc(sizeof(double) * nb2 * kFan * nnodes, s));
-  CANDMC_RET(cnt.alloc(sizeof(unsigned) * nnodes, s));
+  // counters: cnt (last arriver) or prog + done + ticket + fail (pipelined)
+  const size_t ncnt = pipe ? 2 * (size_t)nnodes + 2 : (size_t)nnodes;
+  CANDMC_RET(cnt.alloc(sizeof(unsigned) * ncnt, s));
   CANDMC_RET(uinv.alloc(sizeof(double) * nb2, s));
-  CANDMC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned) * nnodes, s));
+  CANDMC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned) * ncnt, s));
+  if (pipe) CANDMC_CK(cudaMemsetAsync(rn.p, 0, sizeof(double) * nb2 * nnodes, s));
   a.A = A; a.lda = lda; a.m = m; a.b = b;
   a.Vw = vw.d(); a.Tl = tl.d(); a.Rn = rn.d(); a.Qn = qn.d();
   a.cnt = static_cast<unsigned*>(cnt.p);
+  if (pipe) {
+    a.prog = a.cnt;
+    a.done = a.cnt + nnodes;
+    a.ticket = a.cnt + 2 * nnodes;
+    a.fail = reinterpret_cast<int*>(a.cnt + 2 * nnodes + 1);
+  }
   a.T = T; a.ldT = ldT; a.W = W; a.ldW = ldW; a.Uinv = uinv.d(); a.status = d_status;
   static std::atomic<bool> attr{false};
   if (!attr) {
     CANDMC_CK(cudaFuncSetAttribute(k_hr4_leaf_tree, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    200 * 1024));
+    CANDMC_CK(cudaFuncSetAttribute(k_hr6_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr = true;
   }
   {
     ProfScope ps(CANDMC_KCLASS_PANEL_LEAF, 2.0 * m * b * b, s);
-    k_hr4_leaf_tree<<<(unsigned)P, kLeafThreads, sm, s>>>(a);
+    if (pipe)
+      k_hr6_pipe<<<(unsigned)nnodes, kLeafThreads, sm, s>>>(a);
+    else
+      k_hr4_leaf_tree<<<(unsigned)P, kLeafThreads, sm, s>>>(a);
   }
   CANDMC_CK(cudaGetLastError());
   {

@@ -205,7 +205,9 @@ int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t n, const do
 int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t* n, double* const* A,
                       const int64_t* lda, double* const* B, int nstreams, int use_graph, void* stream);
 
-/* tuning knobs: "leaf_rows" (target rows per TSQR leaf, 32..256, default 64) */
+/* tuning knobs: "leaf_rows" (target rows per TSQR leaf, 32..256, default 64);
+ * "pipe_tree" (1, the default: the levels of the TSQR tree overlap column by
+ * column; 0: level by level) */
 int candmc_set_tuning(const char* key, int64_t value);
 
 /* ---- least-squares request server (no counterpart in the reference) ---------
