@@ -17,14 +17,18 @@
 // FP64 pipe: groups are combined, scaled and subtracted with FP32 TwoSum
 // arithmetic.  Finished rows (the panel's R block) are written back as FP64.
 //
-// Kernel layout (k_oz_mma): one CTA per 128 x 96 output tile and K split,
-// 256 threads.  Operand slices are pre-sliced in global memory in the UMMA
-// "K-major, no swizzle" core-matrix order, so each K16 step of a tile is a
-// contiguous 4 KB (A, 128 rows) and 3 KB (B, 96 rows) block per slice;
-// threads copy them with cp.async into a 3-stage shared-memory ring, one
-// elected thread issues the 28 tcgen05.mma of a step and commits them to the
-// stage's mbarrier.  Every wait is bounded; a wait that runs out sets the
-// status word, the CTA drains and frees its TMEM and returns.
+// Kernel layout (k_oz_mma): persistent CTAs (at most one per SM) over work
+// items of one 128 x 96 output tile and K range each; 10 warps.  Operand
+// slices are pre-sliced in global memory in the UMMA "K-major, no swizzle"
+// core-matrix order, so each K16 step of a tile is a contiguous 4 KB (A, 128
+// rows) and 3 KB (B, 96 rows) block per slice: a producer warp streams them
+// with bulk asynchronous copies into a 4-stage shared-memory ring, an MMA
+// warp issues the 28 tcgen05.mma of a step and commits them to the stage's
+// "empty" mbarrier (and, at the end of an exact-accumulation group, to the
+// epilogue's "full" mbarrier), and eight epilogue warps drain TMEM, release it
+// and combine in df64 while the next group's MMAs run.  Every wait is
+// bounded; a wait that runs out sets the status word, the roles stop, the
+// MMA warp waits for its last MMAs, and the CTA frees its TMEM and returns.
 #include <cuda_bf16.h>
 #include <math.h>
 
@@ -38,7 +42,7 @@ constexpr int OZ_S = 7;           // slices per operand
 constexpr int OZ_G = 5;           // TMEM accumulator groups
 constexpr int OZ_M = 128;         // tile rows (TMEM lanes)
 constexpr int OZ_N = 96;          // tile columns
-constexpr int OZ_STAGES = 3;
+constexpr int OZ_STAGES = 4;
 constexpr int OZ_ABYTES = OZ_M * 16 * 2;               // one slice, one K16 step
 constexpr int OZ_BBYTES = OZ_N * 16 * 2;
 constexpr int OZ_STAGE_BYTES = OZ_S * (OZ_ABYTES + OZ_BBYTES);
@@ -225,21 +229,8 @@ struct OzArgs {
   int64_t Mvalid, Nvalid;
   int64_t fp64_rows;         // mode 1: rows < fp64_rows are written as FP64 (final)
   int* status;
+  int64_t n_mt, n_nt, n_ks;  // work items: M tiles x N tiles x K splits
 };
-
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
-  for (long it = 0; it < OZ_WAIT_LIMIT; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, q;\n\t}"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
 
 __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
   // K-major, no swizzle: LBO = 128 B (next 8 K elements), SBO = 256 B (next 8 rows)
@@ -259,31 +250,98 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t saddr, const void* g) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(g) : "memory");
+
+constexpr int OZ_WARPS = 10;              // producer, MMA issuer, 8 epilogue warps
+constexpr int OZ_THREADS = OZ_WARPS * 32;
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs a) {
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+               : "memory");
+}
+
+// bulk global -> shared copy (16-byte aligned, multiple of 16 bytes) that
+// signals the byte count on the stage's mbarrier
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, unsigned bytes, uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(smem_u32(b))
+      : "memory");
+}
+
+// bounded wait; gives up early when another role of the CTA failed
+__device__ __forceinline__ bool oz_wait(uint64_t* b, uint32_t parity, volatile int* fail) {
+  const uint32_t addr = smem_u32(b);
+  for (long it = 0; it < OZ_WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 63) == 63 && *fail) return false;
+  }
+  *fail = 1;
+  return false;
+}
+
+// Work item w of a launch: (M tile, N tile, K range).  M tiles run fastest so
+// that consecutive items of a CTA share the B operand's slices in L2.
+struct OzItem {
+  int64_t m0, n0, kbeg, kend;
+  int split;
+};
+
+__device__ __forceinline__ OzItem oz_item(const OzArgs& a, int64_t w) {
+  OzItem it;
+  const int64_t mt = w % a.n_mt, rest = w / a.n_mt;
+  const int64_t nt = rest % a.n_nt, ks = rest / a.n_nt;
+  it.m0 = mt * OZ_M;
+  it.n0 = nt * OZ_N;
+  it.kbeg = ks * a.k_per_cta;
+  it.kend = (it.kbeg + a.k_per_cta < a.Kpad) ? it.kbeg + a.k_per_cta : a.Kpad;
+  it.split = (int)ks;
+  return it;
+}
+
+// Persistent, warp-specialised emulated-FP64 contraction.  Warp 0 streams the
+// operands' pre-sliced K16 blocks into a ring of OZ_STAGES stages with bulk
+// copies; warp 1 issues the 28 slice-pair MMAs of a stage into the five TMEM
+// accumulator groups and commits them (freeing the stage, and at the end of
+// an exact-accumulation group, handing the accumulators to the epilogue);
+// warps 2..9 read the accumulators (warp w owns TMEM lanes 32 (w % 4) .. +31,
+// half (w - 2) / 4 of the columns), release them, and combine them in df64.
+template <int MODE>
+__global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
   extern __shared__ __align__(1024) unsigned char oz_smem[];
-  __shared__ __align__(8) uint64_t mbar[OZ_STAGES];
+  __shared__ __align__(8) uint64_t full_b[OZ_STAGES], empty_b[OZ_STAGES], acc_full, acc_empty, fin;
   __shared__ uint32_t tmem_base_s;
-  __shared__ int s_fail;
+  __shared__ volatile int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   unsigned char* ring = (unsigned char*)(((uintptr_t)oz_smem + 1023) & ~(uintptr_t)1023);
-
-  const int64_t m0 = (int64_t)blockIdx.x * OZ_M;
-  const int64_t n0 = (int64_t)blockIdx.y * OZ_N;
-  const int64_t kbeg = (int64_t)blockIdx.z * a.k_per_cta;
-  const int64_t kend = (kbeg + a.k_per_cta < a.Kpad) ? kbeg + a.k_per_cta : a.Kpad;
-  const int nsteps = (int)((kend - kbeg) / 16);
+  const int64_t nitems = a.n_mt * a.n_nt * a.n_ks;
   const int steps_per_group = (int)(a.kgroup / 16);
 
   if (tid == 0) {
-    for (int s = 0; s < OZ_STAGES; ++s)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[s])));
+    for (int st = 0; st < OZ_STAGES; ++st) {
+      mbar_init(&full_b[st], 1);
+      mbar_init(&empty_b[st], 1);
+    }
+    mbar_init(&acc_full, 1);
+    mbar_init(&acc_empty, 8);
+    mbar_init(&fin, 1);
     s_fail = 0;
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base_s)),
                  "r"(512));
@@ -295,166 +353,163 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs a) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base_s;
 
-  // loader: K16 step t into stage t % OZ_STAGES
-  auto load_step = [&](int t) {
-    const int st = t % OZ_STAGES;
-    const int64_t kb = (kbeg >> 4) + t;   // K16 block index
-    unsigned char* sbase = ring + (size_t)st * OZ_STAGE_BYTES;
-    // A: OZ_S slices x 4096 B; B: OZ_S slices x 3072 B, 16 B per copy
-    constexpr int ACH = OZ_ABYTES / 16, BCH = OZ_BBYTES / 16;
-    for (int idx = tid; idx < OZ_S * (ACH + BCH); idx += kThreads) {
-      int s, c;
-      const unsigned char* g;
-      uint32_t dst;
-      if (idx < OZ_S * ACH) {
-        s = idx / ACH;
-        c = idx % ACH;
-        g = (const unsigned char*)(a.As + s * a.AR * a.Kpad + kb * a.AR * 16 + (m0 >> 3) * 128) + c * 16;
-        dst = smem_u32(sbase + s * OZ_ABYTES + c * 16);
-      } else {
-        int j = idx - OZ_S * ACH;
-        s = j / BCH;
-        c = j % BCH;
-        g = (const unsigned char*)(a.Bs + s * a.BR * a.Kpad + kb * a.BR * 16 + (n0 >> 3) * 128) + c * 16;
-        dst = smem_u32(sbase + OZ_S * OZ_ABYTES + s * OZ_BBYTES + c * 16);
-      }
-      cp_async16(dst, g);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  };
-
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_N >> 3) << 17) |
-                         ((uint32_t)(OZ_M >> 4) << 24);
-  // df64 accumulators of mode 0: this thread's row, 48 columns (half of the tile)
-  const int q = warp & 3;            // TMEM lane quarter
-  const int half = warp >> 2;        // column half
-  const int row = q * 32 + lane;
-  f2 acc[48];
-#pragma unroll
-  for (int j = 0; j < 48; ++j) acc[j] = {0.0f, 0.0f};
-
-  for (int t = 0; t < OZ_STAGES - 1 && t < nsteps; ++t) load_step(t);
-  // MMA completion is tracked by thread 0 alone, in step order: step u is the
-  // (u / OZ_STAGES)-th commit on stage u % OZ_STAGES.
-  int next_done = 0;
-  auto ensure_done = [&](int u) -> bool {
-    for (; next_done <= u; ++next_done) {
-      if (!mbar_wait(smem_u32(&mbar[next_done % OZ_STAGES]), (uint32_t)((next_done / OZ_STAGES) & 1)))
-        return false;
-    }
-    return true;
-  };
-  int last_issued = -1;
-  for (int t = 0; t < nsteps; ++t) {
-    const int st = t % OZ_STAGES;
-    // the loads of step t are in the oldest outstanding group
-    if (t + 1 < nsteps)
-      asm volatile("cp.async.wait_group %0;" ::"n"(OZ_STAGES - 2) : "memory");
-    else
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    const int step_in_group = t % steps_per_group;
-    const bool group_end = (step_in_group == steps_per_group - 1) || (t == nsteps - 1);
-    const int refill = (t + OZ_STAGES - 1 < nsteps) ? t + OZ_STAGES - 1 : -1;
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      unsigned char* sbase = ring + (size_t)st * OZ_STAGE_BYTES;
-      bool first_of_group[OZ_G];
-#pragma unroll
-      for (int g = 0; g < OZ_G; ++g) first_of_group[g] = (step_in_group == 0);
-#pragma unroll
-      for (int i = 0; i < OZ_S; ++i) {
-#pragma unroll
-        for (int j = 0; j < OZ_S; ++j) {
-          if (i + j >= OZ_S) continue;
-          const int g = (i + j < OZ_G - 1) ? i + j : OZ_G - 1;
-          const uint64_t ad = make_desc(smem_u32(sbase + i * OZ_ABYTES));
-          const uint64_t bd = make_desc(smem_u32(sbase + OZ_S * OZ_ABYTES + j * OZ_BBYTES));
-          const uint32_t dt = tmem + (uint32_t)(g * OZ_N);
-          const uint32_t accum = first_of_group[g] ? 0u : 1u;
-          first_of_group[g] = false;
-          asm volatile(
-              "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
-              "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+  if (warp == 0) {
+    // ---------------- producer
+    if (lane == 0) {
+      int64_t gs = 0;   // stage fills issued by this CTA
+      for (int64_t w = blockIdx.x; w < nitems && !s_fail; w += gridDim.x) {
+        const OzItem it = oz_item(a, w);
+        for (int64_t kb = it.kbeg >> 4; kb < (it.kend >> 4); ++kb, ++gs) {
+          const int st = (int)(gs % OZ_STAGES);
+          if (!oz_wait(&empty_b[st], (uint32_t)(((gs / OZ_STAGES) & 1) ^ 1), &s_fail)) break;
+          mbar_expect_tx(&full_b[st], (unsigned)OZ_STAGE_BYTES);
+          unsigned char* sb = ring + (size_t)st * OZ_STAGE_BYTES;
+#pragma unroll 1
+          for (int sl = 0; sl < OZ_S; ++sl) {
+            bulk_g2s(smem_u32(sb + sl * OZ_ABYTES),
+                     a.As + (int64_t)sl * a.AR * a.Kpad + kb * a.AR * 16 + (it.m0 >> 3) * 128,
+                     (unsigned)OZ_ABYTES, &full_b[st]);
+            bulk_g2s(smem_u32(sb + OZ_S * OZ_ABYTES + sl * OZ_BBYTES),
+                     a.Bs + (int64_t)sl * a.BR * a.Kpad + kb * a.BR * 16 + (it.n0 >> 3) * 128,
+                     (unsigned)OZ_BBYTES, &full_b[st]);
+          }
         }
       }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(&mbar[st]))
-          : "memory");
-      last_issued = t;
-      bool good = true;
-      // the stage refilled next was read by step t-1; step t's MMAs keep the pipe busy meanwhile
-      if (refill >= 0 && t >= 1) good = ensure_done(t - 1);
-      if (good && group_end) good = ensure_done(t);
-      if (!good) s_fail = 1;
     }
-    __syncthreads();
-    if (s_fail) break;
-    if (refill >= 0) load_step(refill);
-    if (group_end) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int64_t grp = (kbeg + (int64_t)t * 16) / a.kgroup;
-      const int64_t gm = m0 + row;
-      const int eA = (gm < a.AR) ? a.eA[grp * a.AR + gm] : 0;
+  } else if (warp == 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_N >> 3) << 17) |
+                             ((uint32_t)(OZ_M >> 4) << 24);
+      int64_t gs = 0, ngroups = 0;
+      for (int64_t w = blockIdx.x; w < nitems && !s_fail; w += gridDim.x) {
+        const OzItem it = oz_item(a, w);
+        const int nsteps = (int)((it.kend - it.kbeg) >> 4);
+        for (int t = 0; t < nsteps && !s_fail; ++t, ++gs) {
+          const int sig = t % steps_per_group;
+          if (sig == 0) {
+            // the epilogue has read the previous group's accumulators
+            if (!oz_wait(&acc_empty, (uint32_t)((ngroups & 1) ^ 1), &s_fail)) break;
+          }
+          const int st = (int)(gs % OZ_STAGES);
+          if (!oz_wait(&full_b[st], (uint32_t)((gs / OZ_STAGES) & 1), &s_fail)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          unsigned char* sb = ring + (size_t)st * OZ_STAGE_BYTES;
+          // the first product into each accumulator in a group's first step overwrites it
+          bool first_of_group[OZ_G];
 #pragma unroll
-      for (int c16 = 0; c16 < 3; ++c16) {
-        const int cbase = half * 48 + c16 * 16;
-        float gv[OZ_G][16];
+          for (int g = 0; g < OZ_G; ++g) first_of_group[g] = (sig == 0);
 #pragma unroll
-        for (int g = 0; g < OZ_G; ++g)
-          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * OZ_N + cbase), gv[g]);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          for (int i = 0; i < OZ_S; ++i) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int64_t gn = n0 + cbase + j;
-          const int eB = (gn < a.BR) ? a.eB[grp * a.BR + gn] : 0;
-          f2 sv = two_sum(gv[0][j], gv[1][j]);
-          sv = fast_two_sum(sv.h, sv.l);
-          sv = df_add_f(sv, gv[2][j]);
-          sv = df_add_f(sv, gv[3][j]);
-          sv = df_add_f(sv, gv[4][j]);
-          const int sh = eA + eB - 16;
-          sv.h = ldexpf(sv.h, sh);
-          sv.l = ldexpf(sv.l, sh);
-          if (a.mode == 0) {
-            acc[c16 * 16 + j] = df_add(acc[c16 * 16 + j], sv);
-          } else if (gm < a.Mvalid && gn < a.Nvalid) {
+            for (int j = 0; j < OZ_S; ++j) {
+              if (i + j >= OZ_S) continue;
+              const int g = (i + j < OZ_G - 1) ? i + j : OZ_G - 1;
+              const uint64_t ad = make_desc(smem_u32(sb + i * OZ_ABYTES));
+              const uint64_t bd = make_desc(smem_u32(sb + OZ_S * OZ_ABYTES + j * OZ_BBYTES));
+              const uint32_t dt = tmem + (uint32_t)(g * OZ_N);
+              const uint32_t accum = first_of_group[g] ? 0u : 1u;
+              first_of_group[g] = false;
+              asm volatile(
+                  "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
+                  "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+            }
+          }
+          // the stage is free once these MMAs have read it
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                  smem_u32(&empty_b[st]))
+              : "memory");
+          if (sig == steps_per_group - 1 || t == nsteps - 1) {
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    smem_u32(&acc_full))
+                : "memory");
+            ++ngroups;
+          }
+        }
+      }
+      // every MMA this thread issued has completed before TMEM is released
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&fin))
+                   : "memory");
+      volatile int dummy = 0;
+      oz_wait(&fin, 0u, &dummy);
+    }
+  } else {
+    // ---------------- epilogue: warps 2..9
+    const int q = warp & 3;                // TMEM lane quarter this warp may access
+    const int half = (warp - 2) >> 2;      // column half
+    const int row = q * 32 + lane;
+    int64_t ngroups = 0;
+    f2 acc[48];   // MODE 0: partial sums over the item's K range; MODE 1: this group's product
+    for (int64_t w = blockIdx.x; w < nitems && !s_fail; w += gridDim.x) {
+      const OzItem it = oz_item(a, w);
+      const int nsteps = (int)((it.kend - it.kbeg) >> 4);
+      const int64_t gm = it.m0 + row;
+#pragma unroll
+      for (int j = 0; j < 48; ++j) acc[j] = {0.0f, 0.0f};
+      for (int t0 = 0; t0 < nsteps; t0 += steps_per_group) {
+        if (!oz_wait(&acc_full, (uint32_t)(ngroups & 1), &s_fail)) break;
+        ++ngroups;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int64_t grp = (it.kbeg + (int64_t)t0 * 16) / a.kgroup;
+        const int eA = (gm < a.AR) ? a.eA[grp * a.AR + gm] : 0;
+#pragma unroll
+        for (int c16 = 0; c16 < 3; ++c16) {
+          const int cbase = half * 48 + c16 * 16;
+          float gv[OZ_G][16];
+#pragma unroll
+          for (int g = 0; g < OZ_G; ++g)
+            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * OZ_N + cbase), gv[g]);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int64_t gn = it.n0 + cbase + j;
+            const int eB = (gn < a.BR) ? a.eB[grp * a.BR + gn] : 0;
+            f2 v = two_sum(gv[0][j], gv[1][j]);
+            v = fast_two_sum(v.h, v.l);
+            v = df_add_f(v, gv[2][j]);
+            v = df_add_f(v, gv[3][j]);
+            v = df_add_f(v, gv[4][j]);
+            const int sh = eA + eB - 16;
+            const f2 sv = {ldexpf(v.h, sh), ldexpf(v.l, sh)};
+            if (MODE == 0) acc[c16 * 16 + j] = df_add(acc[c16 * 16 + j], sv);
+            else acc[c16 * 16 + j] = sv;
+          }
+        }
+        // the accumulators are free for the next group
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty);
+        if (MODE == 1 && gm < a.Mvalid) {
+#pragma unroll
+          for (int j = 0; j < 48; ++j) {
+            const int64_t gn = it.n0 + half * 48 + j;
+            if (gn >= a.Nvalid) continue;
             const int64_t ci = gn * a.ldc + gm;
             const float2 c = a.C[ci];
-            f2 r = df_add({c.x, c.y}, {-sv.h, -sv.l});
+            const f2 r = df_add({c.x, c.y}, {-acc[j].h, -acc[j].l});
             if (gm < a.fp64_rows) a.C64[ci] = df_to_double(r);
             else a.C[ci] = make_float2(r.h, r.l);
           }
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-    }
-  }
-  if (s_fail) {
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
-    if (tid == 0) {
-      atomicExch(a.status, CANDMC_ERR_TIMEOUT);
-      // let in-flight MMAs finish (bounded) before TMEM is released
-      if (last_issued >= 0) ensure_done(last_issued);
-    }
-  } else if (a.mode == 0) {
-    const int64_t gm = m0 + row;
-    float2* out = a.part + (int64_t)blockIdx.z * a.Nvalid * a.AR;
-    if (gm < a.AR) {
+      if (MODE == 0 && !s_fail && gm < a.AR) {
+        float2* out = a.part + (int64_t)it.split * a.Nvalid * a.AR;
 #pragma unroll
-      for (int j = 0; j < 48; ++j) {
-        const int64_t gn = n0 + half * 48 + j;
-        if (gn < a.Nvalid) out[gn * a.AR + gm] = make_float2(acc[j].h, acc[j].l);
+        for (int j = 0; j < 48; ++j) {
+          const int64_t gn = it.n0 + half * 48 + j;
+          if (gn < a.Nvalid) out[gn * a.AR + gm] = make_float2(acc[j].h, acc[j].l);
+        }
       }
     }
   }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0)
+  if (s_fail && tid == 0) atomicExch(a.status, CANDMC_ERR_TIMEOUT);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
@@ -542,15 +597,25 @@ static int launch_slice_krow(SliceSrc src, int64_t n0, int64_t Nvalid, int64_t K
   return CANDMC_OK;
 }
 
-static int launch_oz(const OzArgs& a, unsigned gm, unsigned gn, unsigned gk, int cls, double flops,
+// one persistent CTA per SM at most, each taking every gridDim-th work item
+static int launch_oz(OzArgs a, unsigned gm, unsigned gn, unsigned gk, int cls, double flops,
                      cudaStream_t s) {
   static std::atomic<bool> attr{false};
   if (!attr) {
-    CANDMC_CK(cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
+    CANDMC_CK(cudaFuncSetAttribute(k_oz_mma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
+    CANDMC_CK(cudaFuncSetAttribute(k_oz_mma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
     attr = true;
   }
+  a.n_mt = gm;
+  a.n_nt = gn;
+  a.n_ks = gk;
+  const int64_t items = (int64_t)gm * gn * gk;
+  const unsigned grid = (unsigned)std::min<int64_t>(items, num_sms_oz());
   ProfScope ps(cls, flops, s);
-  k_oz_mma<<<dim3(gm, gn, gk), kThreads, OZ_SMEM, s>>>(a);
+  if (a.mode == 0)
+    k_oz_mma<0><<<grid, OZ_THREADS, OZ_SMEM, s>>>(a);
+  else
+    k_oz_mma<1><<<grid, OZ_THREADS, OZ_SMEM, s>>>(a);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
 }
