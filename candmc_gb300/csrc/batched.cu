@@ -133,6 +133,11 @@ extern "C" int candmc_set_tuning(const char* key, int64_t value) {
     g_leaf_rows = value;
     return CANDMC_OK;
   }
+  if (std::string(key) == "oz_reserve_sms") {
+    if (value < 0 || value > 144) return set_error(CANDMC_ERR_ARG, "oz_reserve_sms in [0, 144]");
+    g_oz_reserve_sms = (int)value;
+    return CANDMC_OK;
+  }
   if (std::string(key) == "pipe_tree") {
     if (value != 0 && value != 1) return set_error(CANDMC_ERR_ARG, "pipe_tree is 0 or 1");
     g_pipe_tree = (int)value;

@@ -218,6 +218,17 @@ static int check_form(int precision, int64_t b, bool* pair) {
 }
 
 // High-priority, non-blocking side stream per device for the lookahead panels.
+static int device_sms() {
+  static std::atomic<int> n{0};
+  if (n.load() == 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    n = v > 0 ? v : 148;
+  }
+  return n.load();
+}
+
 // One lookahead stream per host thread and device, so that factorizations
 // issued concurrently from several threads (the request server's workers) do
 // not queue their panels behind one another.
@@ -268,6 +279,12 @@ int qr_2d_pipe_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int*
                    cudaStream_t s, double* Tall) {
   bool oz;
   CANDMC_RET(check_form(precision, b, &oz));
+  // keep some SMs free of the persistent trailing-update CTAs for the panel stream
+  struct CapScope {
+    int saved;
+    explicit CapScope(int cap) : saved(t_oz_cap) { t_oz_cap = cap; }
+    ~CapScope() { t_oz_cap = saved; }
+  } cap_scope(g_oz_reserve_sms > 0 ? std::max(1, device_sms() - g_oz_reserve_sms) : 0);
   cudaStream_t sp = panel_stream();
   if (!sp) return set_error(CANDMC_ERR_CUDA, "could not create the lookahead stream");
   EventRing evs;

@@ -32,6 +32,12 @@ int hr_direct(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, 
 // tsqr4.cu: direct TSQR-HR with a fan-in-4 tree and compact-WY Q blocks.
 extern int64_t g_leaf_rows;
 extern int g_pipe_tree;
+// SMs left free of persistent Ozaki CTAs while a lookahead factorization runs,
+// so the panel stream is not starved (tuning knob "oz_reserve_sms")
+extern int g_oz_reserve_sms;
+// per host thread: > 0 caps the persistent Ozaki grid (set for the duration
+// of a lookahead factorization)
+extern thread_local int t_oz_cap;
 int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
                int64_t ldW, int* d_status, cudaStream_t s);
 

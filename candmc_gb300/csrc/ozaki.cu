@@ -597,7 +597,11 @@ static int launch_slice_krow(SliceSrc src, int64_t n0, int64_t Nvalid, int64_t K
   return CANDMC_OK;
 }
 
-// one persistent CTA per SM at most, each taking every gridDim-th work item
+int g_oz_reserve_sms = 16;
+thread_local int t_oz_cap = 0;
+
+// one persistent CTA per SM at most (fewer under a cap), each taking every
+// gridDim-th work item
 static int launch_oz(OzArgs a, unsigned gm, unsigned gn, unsigned gk, int cls, double flops,
                      cudaStream_t s) {
   static std::atomic<bool> attr{false};
@@ -610,7 +614,9 @@ static int launch_oz(OzArgs a, unsigned gm, unsigned gn, unsigned gk, int cls, d
   a.n_nt = gn;
   a.n_ks = gk;
   const int64_t items = (int64_t)gm * gn * gk;
-  const unsigned grid = (unsigned)std::min<int64_t>(items, num_sms_oz());
+  int64_t ctas = num_sms_oz();
+  if (t_oz_cap > 0 && t_oz_cap < ctas) ctas = t_oz_cap;
+  const unsigned grid = (unsigned)std::min<int64_t>(items, ctas);
   ProfScope ps(cls, flops, s);
   if (a.mode == 0)
     k_oz_mma<0><<<grid, OZ_THREADS, OZ_SMEM, s>>>(a);

@@ -207,7 +207,9 @@ int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t* n, double*
 
 /* tuning knobs: "leaf_rows" (target rows per TSQR leaf, 32..256, default 64);
  * "pipe_tree" (1, the default: the levels of the TSQR tree overlap column by
- * column; 0: level by level) */
+ * column; 0: level by level); "oz_reserve_sms" (SMs kept free of the
+ * persistent emulated-FP64 update kernel during QR_2D_pipe, for the panel
+ * stream; default 16) */
 int candmc_set_tuning(const char* key, int64_t value);
 
 /* ---- least-squares request server (no counterpart in the reference) ---------
