@@ -250,6 +250,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                 "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
 
 constexpr int OZ_WARPS = 10;              // producer, MMA issuer, 8 epilogue warps
 constexpr int OZ_THREADS = OZ_WARPS * 32;
@@ -321,6 +331,7 @@ __device__ __forceinline__ OzItem oz_item(const OzArgs& a, int64_t w) {
 // warps 2..9 read the accumulators (warp w owns TMEM lanes 32 (w % 4) .. +31,
 // half (w - 2) / 4 of the columns), release them, and combine them in df64.
 template <int MODE>
+// 10 warps: three warps on some SMSPs, so at most 168 registers per thread
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
   extern __shared__ __align__(1024) unsigned char oz_smem[];
   __shared__ __align__(8) uint64_t full_b[OZ_STAGES], empty_b[OZ_STAGES], acc_full, acc_empty, fin;
@@ -456,27 +467,32 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const int64_t grp = (it.kbeg + (int64_t)t0 * 16) / a.kgroup;
         const int eA = (gm < a.AR) ? a.eA[grp * a.AR + gm] : 0;
+        // drain the five accumulators, 8 columns at a time
 #pragma unroll
-        for (int c16 = 0; c16 < 3; ++c16) {
-          const int cbase = half * 48 + c16 * 16;
-          float gv[OZ_G][16];
+        for (int c8 = 0; c8 < 6; ++c8) {
+          const int cbase = half * 48 + c8 * 8;
+          int eB[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int64_t gn = it.n0 + cbase + j;
+            eB[j] = (gn < a.BR) ? __ldg(a.eB + grp * a.BR + gn) : 0;
+          }
+          float gv[OZ_G][8];
 #pragma unroll
           for (int g = 0; g < OZ_G; ++g)
-            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * OZ_N + cbase), gv[g]);
+            tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * OZ_N + cbase), gv[g]);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int64_t gn = it.n0 + cbase + j;
-            const int eB = (gn < a.BR) ? a.eB[grp * a.BR + gn] : 0;
+          for (int j = 0; j < 8; ++j) {
             f2 v = two_sum(gv[0][j], gv[1][j]);
             v = fast_two_sum(v.h, v.l);
             v = df_add_f(v, gv[2][j]);
             v = df_add_f(v, gv[3][j]);
             v = df_add_f(v, gv[4][j]);
-            const int sh = eA + eB - 16;
+            const int sh = eA + eB[j] - 16;
             const f2 sv = {ldexpf(v.h, sh), ldexpf(v.l, sh)};
-            if (MODE == 0) acc[c16 * 16 + j] = df_add(acc[c16 * 16 + j], sv);
-            else acc[c16 * 16 + j] = sv;
+            if (MODE == 0) acc[c8 * 8 + j] = df_add(acc[c8 * 8 + j], sv);
+            else acc[c8 * 8 + j] = sv;
           }
         }
         // the accumulators are free for the next group
@@ -484,15 +500,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
         __syncwarp();
         if (lane == 0) mbar_arrive(&acc_empty);
         if (MODE == 1 && gm < a.Mvalid) {
+          // C -= product, 8 columns per batch of loads
 #pragma unroll
-          for (int j = 0; j < 48; ++j) {
-            const int64_t gn = it.n0 + half * 48 + j;
-            if (gn >= a.Nvalid) continue;
-            const int64_t ci = gn * a.ldc + gm;
-            const float2 c = a.C[ci];
-            const f2 r = df_add({c.x, c.y}, {-acc[j].h, -acc[j].l});
-            if (gm < a.fp64_rows) a.C64[ci] = df_to_double(r);
-            else a.C[ci] = make_float2(r.h, r.l);
+          for (int c8 = 0; c8 < 6; ++c8) {
+            float2 cv[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int64_t gn = it.n0 + half * 48 + c8 * 8 + j;
+              cv[j] = (gn < a.Nvalid) ? a.C[gn * a.ldc + gm] : make_float2(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int64_t gn = it.n0 + half * 48 + c8 * 8 + j;
+              if (gn >= a.Nvalid) continue;
+              const int64_t ci = gn * a.ldc + gm;
+              const f2 r = df_add({cv[j].x, cv[j].y}, {-acc[c8 * 8 + j].h, -acc[c8 * 8 + j].l});
+              if (gm < a.fp64_rows) a.C64[ci] = df_to_double(r);
+              else a.C[ci] = make_float2(r.h, r.l);
+            }
           }
         }
       }
