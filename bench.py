@@ -305,6 +305,30 @@ class Ctx:
         return self.max_over_ranks(ms), launches, prof, clk
 
 
+def kernel_time_shares(ctx, step):
+    """Share of each kernel class in the summed kernel time of one extra,
+    untimed step profiled on every class (the normalisation of an ncu launch
+    list, so the two can be compared)."""
+    import ctypes
+
+    import torch
+    names = list(ctx.abi.KCLASS)
+    mask = 0
+    for c in names:
+        mask |= 1 << ctx.abi.KCLASS[c]
+    torch.cuda.synchronize()
+    ctx.lib.candmc_profile_begin(mask)
+    step()
+    torch.cuda.synchronize()
+    nc = ctx.abi.NKCLASS
+    kms = (ctypes.c_double * nc)()
+    kwork = (ctypes.c_double * nc)()
+    kl = (ctypes.c_longlong * nc)()
+    ctx.lib.candmc_profile_end(nc, kms, kwork, kl)
+    tot = sum(kms[ctx.abi.KCLASS[c]] for c in names)
+    return {c: kms[ctx.abi.KCLASS[c]] / tot for c in names if tot > 0}
+
+
 def fp64_roof(prof, classes, kernel, step_ms):
     ms = sum(prof[c][0] for c in classes)
     work = sum(prof[c][1] for c in classes)
@@ -510,6 +534,8 @@ def wl_caqr(args, ctx):
         roof = fp64_roof(prof, dom, "k_gemm_f64 (Y^T A split-K partials and A -= Y Z)", t_max)
         roof["traffic"] = traffic_from_profile("gemm_f64_caqr_n16384.md")
 
+    shares = kernel_time_shares(ctx, step)
+    roof["share_of_kernel_time"] = sum(shares.get(c, 0.0) for c in dom)
     bwd = sampled_backward_error(cm, A0, A, b)
 
     e2e = None
@@ -576,6 +602,9 @@ def wl_tsqr_hr(args, ctx):
     roof = fp64_roof(prof, ["panel_leaf", "panel_y"],
                      "k_hr6_pipe (pipelined TSQR tree) or k_hr4_leaf_tree, + k_hr4_form_y (reconstruction, Y)",
                      t_max)
+    roof["traffic"] = traffic_from_profile("tsqr_hr_panel_8192x64.md")
+    shares = kernel_time_shares(ctx, step)
+    roof["share_of_kernel_time"] = shares.get("panel_leaf", 0.0) + shares.get("panel_y", 0.0)
     hbm = measured_peaks().get("hbm_gbs", 6778.0)
     bytes_alg = 16.0 * m * b
     roof["hbm"] = {"achieved_gbs": bytes_alg * args.steps / (t_max / 1e3) / 1e9, "peak_gbs": hbm,
