@@ -939,9 +939,11 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   const int nnodes = total;
   const int64_t Lmax = (m + P - 1) / P;
   const size_t nb2 = (size_t)b * b;
-  // shared block: rows padded to whole warps of lanes, at least the 4 x 32
-  // rows of a tree node
-  const int64_t ldS = std::max<int64_t>((Lmax + 31) / 32 * 32, kFan * 32);
+  // shared block: rows padded to the row slots of the factor instantiation
+  // that runs (1..4 slots of 32 rows, or 8 for leaves of more than 128 rows),
+  // and at least the 4 x 32 rows of a tree node
+  const int64_t slots = (Lmax + 31) / 32;
+  const int64_t ldS = std::max<int64_t>(32 * (slots <= 4 ? slots : 8), kFan * 32);
   if (ldS > 32 * kMaxR) return CANDMC_ERR_ARG;
   a.ldS = (int)ldS;
   // block + G + T + tri-inverse workspace; the root reuses the front of the

@@ -79,9 +79,11 @@ def test_batched_rejects_wide_problem(cm):
         cm.batched_ls([A], [b])
 
 
-def test_leaf_rows_tuning_keeps_results(cm):
-    host = make(fx.batched_problems(8, seed=9, m_lo=2048, m_hi=16384, widths=(32, 64)))
-    for leaf in (64, 256):
+@pytest.mark.parametrize("m_lo,m_hi", [(2048, 16384), (160, 2000)])
+def test_leaf_rows_tuning_keeps_results(cm, m_lo, m_hi):
+    # (160, 2000): leaves of 129..224 rows, whose row slots round up to the 8-slot factor
+    host = make(fx.batched_problems(12, seed=9, m_lo=m_lo, m_hi=m_hi, widths=(8, 32, 64, 128)))
+    for leaf in (64, 96, 256):
         cm.set_tuning("leaf_rows", leaf)
         As, Bs = to_dev(host)
         xs = cm.batched_ls(As, Bs, nstreams=4)
