@@ -138,6 +138,11 @@ extern "C" int candmc_set_tuning(const char* key, int64_t value) {
     g_oz_reserve_sms = (int)value;
     return CANDMC_OK;
   }
+  if (std::string(key) == "pipe_leaf_rows") {
+    if (value < 32 || value > 256) return set_error(CANDMC_ERR_ARG, "pipe_leaf_rows in [32, 256]");
+    g_pipe_leaf_rows = value;
+    return CANDMC_OK;
+  }
   if (std::string(key) == "pipe_tree") {
     if (value != 0 && value != 1) return set_error(CANDMC_ERR_ARG, "pipe_tree is 0 or 1");
     g_pipe_tree = (int)value;

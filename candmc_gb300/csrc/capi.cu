@@ -280,11 +280,19 @@ int qr_2d_pipe_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int*
   bool oz;
   CANDMC_RET(check_form(precision, b, &oz));
   // keep some SMs free of the persistent trailing-update CTAs for the panel stream
+  // and factor its panels with taller leaves (fewer CTAs compete with the update)
   struct CapScope {
     int saved;
-    explicit CapScope(int cap) : saved(t_oz_cap) { t_oz_cap = cap; }
-    ~CapScope() { t_oz_cap = saved; }
-  } cap_scope(g_oz_reserve_sms > 0 ? std::max(1, device_sms() - g_oz_reserve_sms) : 0);
+    int64_t saved_leaf;
+    CapScope(int cap, int64_t leaf) : saved(t_oz_cap), saved_leaf(t_leaf_rows) {
+      t_oz_cap = cap;
+      t_leaf_rows = leaf;
+    }
+    ~CapScope() {
+      t_oz_cap = saved;
+      t_leaf_rows = saved_leaf;
+    }
+  } cap_scope(g_oz_reserve_sms > 0 ? std::max(1, device_sms() - g_oz_reserve_sms) : 0, g_pipe_leaf_rows);
   cudaStream_t sp = panel_stream();
   if (!sp) return set_error(CANDMC_ERR_CUDA, "could not create the lookahead stream");
   EventRing evs;

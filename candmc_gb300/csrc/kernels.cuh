@@ -32,6 +32,10 @@ int hr_direct(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, 
 // tsqr4.cu: direct TSQR-HR with a fan-in-4 tree and compact-WY Q blocks.
 extern int64_t g_leaf_rows;
 extern int g_pipe_tree;
+// leaf height of the panels factored by the lookahead (tuning knob
+// "pipe_leaf_rows"), and the per-host-thread override it sets (0: none)
+extern int64_t g_pipe_leaf_rows;
+extern thread_local int64_t t_leaf_rows;
 // SMs left free of persistent Ozaki CTAs while a lookahead factorization runs,
 // so the panel stream is not starved (tuning knob "oz_reserve_sms")
 extern int g_oz_reserve_sms;

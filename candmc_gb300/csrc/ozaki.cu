@@ -622,7 +622,7 @@ static int launch_slice_krow(SliceSrc src, int64_t n0, int64_t Nvalid, int64_t K
   return CANDMC_OK;
 }
 
-int g_oz_reserve_sms = 16;
+int g_oz_reserve_sms = 32;
 thread_local int t_oz_cap = 0;
 
 // one persistent CTA per SM at most (fewer under a cap), each taking every

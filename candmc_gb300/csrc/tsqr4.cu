@@ -36,6 +36,8 @@ constexpr int kFan = 4;
 
 // Target rows per TSQR leaf (tuning knob, candmc_set_tuning("leaf_rows", v)).
 int64_t g_leaf_rows = 64;
+int64_t g_pipe_leaf_rows = 128;
+thread_local int64_t t_leaf_rows = 0;
 // Pipelined tree on/off (tuning knob, candmc_set_tuning("pipe_tree", 0|1)).
 int g_pipe_tree = 1;
 constexpr int kTriScratch = 512 + kDirectB * kDirectB;   // h4_tri_inv workspace (doubles)
@@ -920,7 +922,8 @@ __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
 int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
                int64_t ldW, int* d_status, cudaStream_t s) {
   if (b < 1 || b > kDirectB || m < b) return CANDMC_ERR_ARG;
-  const int64_t leaf_rows = std::max<int64_t>(32, std::min<int64_t>(g_leaf_rows, 256));
+  const int64_t want = t_leaf_rows > 0 ? t_leaf_rows : g_leaf_rows;
+  const int64_t leaf_rows = std::max<int64_t>(32, std::min<int64_t>(want, 256));
   // leaves of at most leaf_rows rows and at least b rows
   int64_t P = std::max<int64_t>(1, std::min<int64_t>((m + leaf_rows - 1) / leaf_rows, m / b));
   if (P > (1 << 24)) return CANDMC_ERR_ARG;

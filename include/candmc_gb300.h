@@ -209,7 +209,8 @@ int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t* n, double*
  * "pipe_tree" (1, the default: the levels of the TSQR tree overlap column by
  * column; 0: level by level); "oz_reserve_sms" (SMs kept free of the
  * persistent emulated-FP64 update kernel during QR_2D_pipe, for the panel
- * stream; default 16) */
+ * stream; default 32); "pipe_leaf_rows" (leaf height of the panels QR_2D_pipe
+ * factors, 32..256, default 128) */
 int candmc_set_tuning(const char* key, int64_t value);
 
 /* ---- least-squares request server (no counterpart in the reference) ---------
