@@ -337,6 +337,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
   __shared__ __align__(8) uint64_t full_b[OZ_STAGES], empty_b[OZ_STAGES], acc_full, acc_empty, fin;
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int s_fail;
+  __shared__ int s_eb[8][48];   // per epilogue warp: the column exponents of its group
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   unsigned char* ring = (unsigned char*)(((uintptr_t)oz_smem + 1023) & ~(uintptr_t)1023);
   const int64_t nitems = a.n_mt * a.n_nt * a.n_ks;
@@ -467,16 +468,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const int64_t grp = (it.kbeg + (int64_t)t0 * 16) / a.kgroup;
         const int eA = (gm < a.AR) ? a.eA[grp * a.AR + gm] : 0;
+        // this warp's 48 column exponents, staged once per group
+        int* eb = s_eb[warp - 2];
+        for (int c = lane; c < 48; c += 32) {
+          const int64_t gn = it.n0 + half * 48 + c;
+          eb[c] = (gn < a.BR) ? __ldg(a.eB + grp * a.BR + gn) : 0;
+        }
+        __syncwarp();
         // drain the five accumulators, 8 columns at a time
 #pragma unroll
         for (int c8 = 0; c8 < 6; ++c8) {
           const int cbase = half * 48 + c8 * 8;
           int eB[8];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int64_t gn = it.n0 + cbase + j;
-            eB[j] = (gn < a.BR) ? __ldg(a.eB + grp * a.BR + gn) : 0;
-          }
+          for (int j = 0; j < 8; ++j) eB[j] = eb[c8 * 8 + j];
           float gv[OZ_G][8];
 #pragma unroll
           for (int g = 0; g < OZ_G; ++g)
@@ -495,7 +500,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
             else acc[c8 * 8 + j] = sv;
           }
         }
-        // the accumulators are free for the next group
+        // the accumulators are free for the next group (and eb may be rewritten)
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncwarp();
         if (lane == 0) mbar_arrive(&acc_empty);
