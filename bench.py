@@ -815,8 +815,10 @@ def wl_batched(args, ctx):
     roof["hbm"] = {"achieved_gbs": by * args.steps / (t_max / 1e3) / 1e9, "peak_gbs": hbm,
                    "frac": by * args.steps / (t_max / 1e3) / 1e9 / hbm,
                    "note": "algorithmic bytes 16 m n per problem (read A, write Y)"}
-    # accuracy on a sample of problems against LAPACK lstsq (numpy)
+    # accuracy on a sample of problems against LAPACK lstsq (numpy), and no
+    # device-side failure recorded by the batched calls
     torch.cuda.synchronize()
+    cm.batched_status()
     rs = np.random.default_rng(0)
     small = [i for i, (m, n) in enumerate(sizes) if m <= 65536]
     errs = []

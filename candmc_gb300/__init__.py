@@ -24,7 +24,7 @@ __all__ = [
     "CandmcError", "colmajor", "empty_colmajor", "hh_recon_qr", "bitree_tsqr", "construct_Q1",
     "compute_invT_from_W", "signed_NLU", "recursive_NLU", "compute_invT_from_Y",
     "compute_invT_from_Y2", "upd_A", "update_A", "QR_2D", "QR_2D_2D", "QR_2D_pipe", "ls_solve",
-    "PRECISIONS", "lib",
+    "batched_ls", "batched_status", "set_tuning", "PRECISIONS", "lib",
 ]
 
 PRECISIONS = {"fp64": 0, "ozaki": 1, "fp32": 2}
@@ -268,6 +268,15 @@ def batched_ls(As, Bs, nstreams=16, use_graph=False, stream=None):
                                   arr(ctypes.c_void_p, pb), int(nstreams), int(bool(use_graph)),
                                   _stream(stream)), "batched_ls")
     return [b[:n] for b, n in zip(Bs, ns)]
+
+
+def batched_status(stream=None):
+    """Wait for the stream and raise CandmcError if a batched call's kernels
+    recorded a failure on this device since the last check (then cleared)."""
+    import ctypes
+    st = ctypes.c_int(0)
+    check(lib().candmc_batched_status(_stream(stream), ctypes.byref(st)), "batched_status")
+    check(st.value, "batched_ls (device status)")
 
 
 def QR_2D_2D(A, b, b_sub, aggreg_Y=None, precision="fp64", stream=None):

@@ -40,6 +40,7 @@ SIGNATURES = {
                         ctypes.c_double, _vp, _vp],
     "candmc_batched_ls": [_i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp],
     "candmc_set_tuning": [ctypes.c_char_p, _i64],
+    "candmc_batched_status": [_vp, _vp],
     "candmc_server_create": [ctypes.c_double, _int, _int, _i64, _int, ctypes.c_double, _vp],
     "candmc_server_submit": [_vp, _vp, _i64, _i64, _i64, _vp, _vp, ctypes.c_double, _vp],
     "candmc_server_wait": [_vp, _i64, ctypes.c_double, _vp],

@@ -46,6 +46,24 @@ struct StreamPool {
 };
 
 static StreamPool g_pool[64];
+
+// Per device: the status word every batched call's kernels record failures in
+// (sticky until candmc_batched_status reads and clears it).  Allocated by the
+// first call on the device, outside any stream capture.
+static int* g_bstatus[64] = {};
+static std::mutex g_bstatus_mu;
+
+static int batched_status_word(int dev, int** out) {
+  std::lock_guard<std::mutex> g(g_bstatus_mu);
+  if (!g_bstatus[dev]) {
+    int* p = nullptr;
+    CANDMC_CK(cudaMalloc(&p, sizeof(int)));
+    CANDMC_CK(cudaMemset(p, 0, sizeof(int)));
+    g_bstatus[dev] = p;
+  }
+  *out = g_bstatus[dev];
+  return CANDMC_OK;
+}
 static std::mutex g_graph_mu;
 struct CachedGraph {
   cudaGraphExec_t exec;
@@ -82,10 +100,10 @@ static int batched_issue(int64_t nprob, const int64_t* m, const int64_t* n, doub
     toff[i] = tsz;
     tsz += n[i] * n[i];
   }
-  DevBuf tbuf, stw;
+  DevBuf tbuf;
   CANDMC_RET(tbuf.alloc(sizeof(double) * std::max<int64_t>(tsz, 1), s));
-  CANDMC_RET(stw.alloc(sizeof(int), s));
-  CANDMC_CK(cudaMemsetAsync(stw.p, 0, sizeof(int), s));
+  int* stword = nullptr;
+  CANDMC_RET(batched_status_word(dev, &stword));
   cudaEvent_t fork;
   CANDMC_CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   CANDMC_CK(cudaEventRecord(fork, s));
@@ -99,7 +117,7 @@ static int batched_issue(int64_t nprob, const int64_t* m, const int64_t* n, doub
     for (int64_t q = k; q < nprob; q += ns) {
       const int64_t i = order[q];
       double* T = tbuf.d() + toff[i];
-      rc = hr_rec(A[i], lda[i], m[i], (int)n[i], T, n[i], static_cast<int*>(stw.p), CANDMC_PREC_FP64, sk);
+      rc = hr_rec(A[i], lda[i], m[i], (int)n[i], T, n[i], stword, CANDMC_PREC_FP64, sk);
       if (rc != CANDMC_OK) break;
       rc = apply_qt(A[i], lda[i], m[i], (int)n[i], T, n[i], B[i], m[i], 1, CANDMC_PREC_FP64, sk);
       if (rc != CANDMC_OK) break;
@@ -125,6 +143,20 @@ static int batched_issue(int64_t nprob, const int64_t* m, const int64_t* n, doub
 }  // namespace candmc
 
 using namespace candmc;
+
+extern "C" int candmc_batched_status(void* stream, int* status) {
+  if (!status) return set_error(CANDMC_ERR_ARG, "batched_status args");
+  int dev = 0, *w = nullptr;
+  CANDMC_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(CANDMC_ERR_ARG, "device index");
+  CANDMC_RET(batched_status_word(dev, &w));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CANDMC_CK(cudaMemcpyAsync(status, w, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CANDMC_CK(cudaStreamSynchronize(s));
+  CANDMC_CK(cudaMemsetAsync(w, 0, sizeof(int), s));
+  CANDMC_CK(cudaStreamSynchronize(s));
+  return CANDMC_OK;
+}
 
 extern "C" int candmc_set_tuning(const char* key, int64_t value) {
   if (!key) return set_error(CANDMC_ERR_ARG, "tuning key");
@@ -161,6 +193,12 @@ extern "C" int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t*
       return set_error(CANDMC_ERR_ARG, "batched_ls: each problem needs 1 <= n <= 128 and m >= n");
   if (nprob == 0) return CANDMC_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  {
+    int dev = 0, *w = nullptr;
+    CANDMC_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(CANDMC_ERR_ARG, "device index");
+    CANDMC_RET(batched_status_word(dev, &w));   // before any capture begins
+  }
   if (!use_graph) return batched_issue(nprob, m, n, A, lda, B, nstreams, s);
   std::vector<int64_t> key;
   key.reserve(6 * nprob + 4);

@@ -205,6 +205,13 @@ int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t n, const do
 int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t* n, double* const* A,
                       const int64_t* lda, double* const* B, int nstreams, int use_graph, void* stream);
 
+/* candmc_batched_status: waits for the stream, then returns in *status the
+ * first failure any batched call's kernels recorded on this device since the
+ * last call (CANDMC_OK if none: e.g. CANDMC_ERR_TIMEOUT, CANDMC_ERR_NUMERIC)
+ * and clears it.  Batched calls return once their work is enqueued, so their
+ * device-side failures surface here. */
+int candmc_batched_status(void* stream, int* status);
+
 /* tuning knobs: "leaf_rows" (target rows per TSQR leaf, 32..256, default 64);
  * "pipe_tree" (1, the default: the levels of the TSQR tree overlap column by
  * column; 0: level by level); "oz_reserve_sms" (SMs kept free of the

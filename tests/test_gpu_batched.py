@@ -39,6 +39,8 @@ def to_dev(host):
 
 
 def check(host, xs):
+    import candmc_gb300 as cm
+    cm.batched_status()   # no device-side failure was recorded
     for (A, b), x in zip(host, xs):
         xo = np.linalg.lstsq(A, b, rcond=None)[0]
         err = np.linalg.norm(x.cpu().numpy() - xo) / np.linalg.norm(xo)
