@@ -177,6 +177,73 @@ __global__ void k_slice_kcol(SliceSrc src, int64_t k0, int64_t Kvalid, int64_t N
   }
 }
 
+// The same slicing with coalesced stores: one CTA per 8 rows n of the operand
+// (one core-matrix row block) and one K group of G <= 128 (a multiple of 16).
+// Warp w reads column n0 + w of the source into shared memory and finds its
+// scale exponent; then, for every K16 block, the 8 x 16 elements of a slice
+// plane are one contiguous 256-byte run of the core-matrix order, which a
+// warp writes with 8-byte stores (4 elements per lane).
+__global__ void __launch_bounds__(256) k_slice_kcol8(SliceSrc src, int64_t k0, int64_t Kvalid,
+                                                     int64_t Nvalid, int64_t Rpad, int64_t Kpad, int G,
+                                                     __nv_bfloat16* out, int* eout) {
+  __shared__ float2 tile[8][128];
+  __shared__ int s_e[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t n0 = (int64_t)blockIdx.x * 8;
+  const int64_t g = blockIdx.y;
+  const int64_t kb0 = g * G;
+  {
+    const int64_t n = n0 + warp;
+    float mx = 0.0f;
+    for (int k = lane; k < G; k += 32) {
+      f2 v = {0.0f, 0.0f};
+      if (n < Nvalid && kb0 + k < Kvalid) v = src_at(src, k0 + kb0 + k, n);
+      tile[warp][k] = make_float2(v.h, v.l);
+      mx = fmaxf(mx, fabsf(v.h));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    // the lo part can push |x| just above |hi|'s bound; leave one ulp of room
+    const int e = scale_exp(mx * (1.0f + 1.0e-6f));
+    if (lane == 0) {
+      s_e[warp] = e;
+      if (n < Rpad) eout[g * Rpad + n] = e;
+    }
+  }
+  __syncthreads();
+  const int64_t plane = Rpad * Kpad;
+  // lane u of a warp: elements 4u .. 4u+3 of a 128-element core-matrix run:
+  // k-half (u / 16), row (u % 16) / 2, k & 7 = 4 (u % 2) .. +3
+  const int u = lane;
+  const int khalf = u >> 4, r = (u & 15) >> 1, k7 = (u & 1) * 4;
+  const int e = s_e[r];
+  for (int blk = warp; blk < G / 16; blk += 8) {
+    float p[4], q[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float2 t = tile[r][blk * 16 + khalf * 8 + k7 + i];
+      p[i] = ldexpf(t.x, 8 - e);
+      q[i] = ldexpf(t.y, 8 - e);
+    }
+    const int64_t base = ((kb0 >> 4) + blk) * (Rpad * 16) + (n0 >> 3) * 128 + 4 * u;
+    float w = 1.0f;
+#pragma unroll
+    for (int sl = 0; sl < OZ_S; ++sl) {
+      __align__(8) __nv_bfloat16 d4[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const f2 sv = two_sum(p[i], q[i]);
+        const float d = rintf(sv.h);
+        d4[i] = __float2bfloat16_rn(d * w);
+        p[i] = (sv.h - d) * 256.0f;
+        q[i] = sv.l * 256.0f;
+      }
+      *reinterpret_cast<uint2*>(out + sl * plane + base) = *reinterpret_cast<const uint2*>(d4);
+      w *= 0.00390625f;
+    }
+  }
+}
+
 // Operand element (n, k) = src(n, k): K runs along the rows of a column-major
 // source (rows n0 + n, columns 0 .. K).  Scale group = the whole row (G = Kpad).
 // A CTA stages 32 rows x Kpad columns through shared memory.
@@ -608,8 +675,14 @@ int from_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s) {
 
 static int launch_slice_kcol(SliceSrc src, int64_t k0, int64_t Kvalid, int64_t Nvalid, int64_t Rpad,
                              int64_t Kpad, int G, __nv_bfloat16* out, int* e, cudaStream_t s) {
-  int64_t warps = Rpad * (Kpad / G);
   ProfScope ps(CANDMC_KCLASS_OZ_SLICE, 8.0 * Nvalid * Kvalid + 14.0 * Rpad * Kpad, s);
+  if (G <= 128 && G % 16 == 0 && Rpad % 8 == 0) {
+    k_slice_kcol8<<<dim3((unsigned)(Rpad / 8), (unsigned)(Kpad / G)), 256, 0, s>>>(src, k0, Kvalid, Nvalid,
+                                                                                  Rpad, Kpad, G, out, e);
+    CANDMC_CK(cudaGetLastError());
+    return CANDMC_OK;
+  }
+  int64_t warps = Rpad * (Kpad / G);
   k_slice_kcol<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(src, k0, Kvalid, Nvalid, Rpad,
                                                                       Kpad, G, out, e);
   CANDMC_CK(cudaGetLastError());
