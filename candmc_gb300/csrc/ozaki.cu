@@ -305,31 +305,70 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
          ((uint64_t)(256 >> 4) << 32) | (1ull << 46);
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-        "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
-}
-
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
+// tcgen05.ld writes its registers asynchronously: they hold the TMEM values
+// only after tcgen05.wait::ld.  The compiler sees no dependence between the
+// two, so the loaded registers are passed through tmem_regs_ready (an empty
+// asm ordered after the wait) before any use.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
                  "=r"(r[7])
                : "r"(taddr));
-#pragma unroll
-  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void tmem_regs_ready(uint32_t* r) {
+  asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]),
+               "+r"(r[7]));
 }
 
 
-constexpr int OZ_WARPS = 10;              // producer, MMA issuer, 8 epilogue warps
+constexpr int OZ_EPI_WARPS = 12;                     // epilogue warps: 4 TMEM lane quarters x column parts
+constexpr int OZ_EPI_COLS = OZ_N * 4 / OZ_EPI_WARPS;  // accumulator columns per epilogue warp
+constexpr int OZ_WARPS = 2 + OZ_EPI_WARPS;             // producer, MMA issuer, epilogue
 constexpr int OZ_THREADS = OZ_WARPS * 32;
+static_assert(OZ_EPI_WARPS % 4 == 0 && OZ_EPI_COLS % 16 == 0, "epilogue split");
+
+// 2^e for -126 <= e <= 127 (a normal float): x * pow2f(e) rounds once, as
+// ldexpf(x, e) does
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+
+// The five accumulators of one output element as one df64 value.  Groups 0..3
+// hold the diagonals i + j = g of the slice products, exact multiples of
+// 2^-8g with |g0| <= 2^23, |g1| <= 2^15, |g2| <= 2^8, |g3| < 1 (digits of at
+// most 8 bits over a 128-row group); group 4 holds the rest, down to about
+// 2^-40.  Rounding g1 and g2 to integers and g3 to a multiple of 2^-16 (the
+// 1.5 * 2^23 and 1.5 * 2^7 shifts) splits them exactly: H = g0 + [g1] + [g2]
+// is an integer below 2^24, M = frac(g1) + frac(g2) + [g3] a multiple of 2^-16
+// below 2 in magnitude, both exact, and only L = (g3 - [g3]) + g4 rounds.  The
+// two fast TwoSums are exact here (H is zero or at least 1 in magnitude), so
+// the result carries about 2^-47 relative error, as a df64 sum of the five.
+// The operations are round-to-nearest intrinsics, which the compiler neither
+// contracts into FMAs nor reorders.
+__device__ __forceinline__ f2 combine_groups(float g0, float g1, float g2, float g3, float g4) {
+  const float kShift = 12582912.0f;   // 1.5 * 2^23: rounds to an integer
+  const float kShift3 = 192.0f;       // 1.5 * 2^7: rounds to a multiple of 2^-16
+  const float r1 = __fsub_rn(__fadd_rn(g1, kShift), kShift);
+  const float r2 = __fsub_rn(__fadd_rn(g2, kShift), kShift);
+  const float r3 = __fsub_rn(__fadd_rn(g3, kShift3), kShift3);
+  const float H = __fadd_rn(__fadd_rn(g0, r1), r2);
+  const float M = __fadd_rn(__fadd_rn(__fsub_rn(g1, r1), __fsub_rn(g2, r2)), r3);
+  const float L = __fadd_rn(__fsub_rn(g3, r3), g4);
+  const float s = __fadd_rn(H, M);
+  const float e = __fsub_rn(M, __fsub_rn(s, H));
+  const float l = __fadd_rn(e, L);
+  const float h = __fadd_rn(s, l);
+  return {h, __fsub_rn(l, __fsub_rn(h, s))};
+}
+
+// x + y without the lo-part TwoSum: relative error of order 2^-46 of |x| + |y|
+__device__ __forceinline__ f2 df_add_sloppy(f2 x, f2 y) {
+  const float s = __fadd_rn(x.h, y.h);
+  const float bb = __fsub_rn(s, x.h);
+  const float e = __fadd_rn(__fsub_rn(x.h, __fsub_rn(s, bb)), __fsub_rn(y.h, bb));
+  const float l = __fadd_rn(e, __fadd_rn(x.l, y.l));
+  const float h = __fadd_rn(s, l);
+  return {h, __fsub_rn(l, __fsub_rn(h, s))};
+}
 
 __device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
@@ -395,16 +434,16 @@ __device__ __forceinline__ OzItem oz_item(const OzArgs& a, int64_t w) {
 // copies; warp 1 issues the 28 slice-pair MMAs of a stage into the five TMEM
 // accumulator groups and commits them (freeing the stage, and at the end of
 // an exact-accumulation group, handing the accumulators to the epilogue);
-// warps 2..9 read the accumulators (warp w owns TMEM lanes 32 (w % 4) .. +31,
-// half (w - 2) / 4 of the columns), release them, and combine them in df64.
+// the epilogue warps 2.. read the accumulators (warp w owns TMEM lanes
+// 32 (w % 4) .. +31 and column part (w - 2) / 4), release them, and combine
+// them in df64.
 template <int MODE>
-// 10 warps: three warps on some SMSPs, so at most 168 registers per thread
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
   extern __shared__ __align__(1024) unsigned char oz_smem[];
   __shared__ __align__(8) uint64_t full_b[OZ_STAGES], empty_b[OZ_STAGES], acc_full, acc_empty, fin;
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int s_fail;
-  __shared__ int s_eb[8][48];   // per epilogue warp: the column exponents of its group
+  __shared__ int s_eb[OZ_EPI_WARPS][OZ_EPI_COLS];   // per epilogue warp: its columns' exponents
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   unsigned char* ring = (unsigned char*)(((uintptr_t)oz_smem + 1023) & ~(uintptr_t)1023);
   const int64_t nitems = a.n_mt * a.n_nt * a.n_ks;
@@ -416,7 +455,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
       mbar_init(&empty_b[st], 1);
     }
     mbar_init(&acc_full, 1);
-    mbar_init(&acc_empty, 8);
+    mbar_init(&acc_empty, OZ_EPI_WARPS);
     mbar_init(&fin, 1);
     s_fail = 0;
   }
@@ -517,54 +556,92 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
       oz_wait(&fin, 0u, &dummy);
     }
   } else {
-    // ---------------- epilogue: warps 2..9
+    // ---------------- epilogue: warps 2 .. 2 + OZ_EPI_WARPS - 1
     const int q = warp & 3;                // TMEM lane quarter this warp may access
-    const int half = (warp - 2) >> 2;      // column half
+    const int part = (warp - 2) >> 2;      // column part
     const int row = q * 32 + lane;
     int64_t ngroups = 0;
-    f2 acc[48];   // MODE 0: partial sums over the item's K range; MODE 1: this group's product
+    f2 acc[OZ_EPI_COLS];   // MODE 0: sums over the item's K range; MODE 1: this group's product
     for (int64_t w = blockIdx.x; w < nitems && !s_fail; w += gridDim.x) {
       const OzItem it = oz_item(a, w);
       const int nsteps = (int)((it.kend - it.kbeg) >> 4);
       const int64_t gm = it.m0 + row;
+      if (MODE == 1 && w + gridDim.x < nitems) {
+        // the next item's C tile streams into L2 while this one is computed
+        const OzItem nx = oz_item(a, w + gridDim.x);
+        const int64_t pm = nx.m0 + row;
+        if (pm < a.Mvalid) {
+          for (int j = 0; j < OZ_EPI_COLS; ++j) {
+            const int64_t gn = nx.n0 + part * OZ_EPI_COLS + j;
+            if (gn < a.Nvalid && (lane & 15) == 0)
+              asm volatile("prefetch.global.L2 [%0];" ::"l"(a.C + gn * a.ldc + pm));
+          }
+        }
+      }
 #pragma unroll
-      for (int j = 0; j < 48; ++j) acc[j] = {0.0f, 0.0f};
+      for (int j = 0; j < OZ_EPI_COLS; ++j) acc[j] = {0.0f, 0.0f};
       for (int t0 = 0; t0 < nsteps; t0 += steps_per_group) {
-        if (!oz_wait(&acc_full, (uint32_t)(ngroups & 1), &s_fail)) break;
-        ++ngroups;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // the group's exponents are loaded while its MMAs run
         const int64_t grp = (it.kbeg + (int64_t)t0 * 16) / a.kgroup;
         const int eA = (gm < a.AR) ? a.eA[grp * a.AR + gm] : 0;
-        // this warp's 48 column exponents, staged once per group
         int* eb = s_eb[warp - 2];
-        for (int c = lane; c < 48; c += 32) {
-          const int64_t gn = it.n0 + half * 48 + c;
+        for (int c = lane; c < OZ_EPI_COLS; c += 32) {
+          const int64_t gn = it.n0 + part * OZ_EPI_COLS + c;
           eb[c] = (gn < a.BR) ? __ldg(a.eB + grp * a.BR + gn) : 0;
         }
         __syncwarp();
+        if (!oz_wait(&acc_full, (uint32_t)(ngroups & 1), &s_fail)) break;
+        ++ngroups;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         // drain the five accumulators, 8 columns at a time
 #pragma unroll
-        for (int c8 = 0; c8 < 6; ++c8) {
-          const int cbase = half * 48 + c8 * 8;
+        for (int c8 = 0; c8 < OZ_EPI_COLS / 8; ++c8) {
+          const int cbase = part * OZ_EPI_COLS + c8 * 8;
           int eB[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) eB[j] = eb[c8 * 8 + j];
-          float gv[OZ_G][8];
+          uint32_t gr[OZ_G][8];
 #pragma unroll
           for (int g = 0; g < OZ_G; ++g)
-            tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * OZ_N + cbase), gv[g]);
+            tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * OZ_N + cbase), gr[g]);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          float gv[OZ_G][8];
+#pragma unroll
+          for (int g = 0; g < OZ_G; ++g) {
+            tmem_regs_ready(gr[g]);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) gv[g][j] = __uint_as_float(gr[g][j]);
+          }
+          // one warp-uniform test: every scale 2^(eA + eB - 16) a normal float
+          bool normal = true;
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            f2 v = two_sum(gv[0][j], gv[1][j]);
-            v = fast_two_sum(v.h, v.l);
-            v = df_add_f(v, gv[2][j]);
-            v = df_add_f(v, gv[3][j]);
-            v = df_add_f(v, gv[4][j]);
-            const int sh = eA + eB[j] - 16;
-            const f2 sv = {ldexpf(v.h, sh), ldexpf(v.l, sh)};
-            if (MODE == 0) acc[c8 * 8 + j] = df_add(acc[c8 * 8 + j], sv);
-            else acc[c8 * 8 + j] = sv;
+            const int e = eA + eB[j] - 16;
+            normal = normal && e >= -126 && e <= 127;
+          }
+          if (__all_sync(0xffffffffu, normal)) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const f2 v = combine_groups(gv[0][j], gv[1][j], gv[2][j], gv[3][j], gv[4][j]);
+              const float f = pow2f(eA + eB[j] - 16);
+              const f2 sv = {__fmul_rn(v.h, f), __fmul_rn(v.l, f)};
+              if (MODE == 0) acc[c8 * 8 + j] = df_add_sloppy(acc[c8 * 8 + j], sv);
+              else acc[c8 * 8 + j] = sv;
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const f2 v = combine_groups(gv[0][j], gv[1][j], gv[2][j], gv[3][j], gv[4][j]);
+              // 2^e as three normal factors (e >= -312 for float inputs): the
+              // partial products stay exact unless the result leaves the range
+              const int e = eA + eB[j] - 16;
+              const int e1 = min(max(e, -126), 127), e2 = min(max(e - e1, -126), 127);
+              const float f1 = pow2f(e1), f2v = pow2f(e2), f3 = pow2f(e - e1 - e2);
+              const f2 sv = {__fmul_rn(__fmul_rn(__fmul_rn(v.h, f1), f2v), f3),
+                             __fmul_rn(__fmul_rn(__fmul_rn(v.l, f1), f2v), f3)};
+              if (MODE == 0) acc[c8 * 8 + j] = df_add_sloppy(acc[c8 * 8 + j], sv);
+              else acc[c8 * 8 + j] = sv;
+            }
           }
         }
         // the accumulators are free for the next group (and eb may be rewritten)
@@ -572,21 +649,21 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
         __syncwarp();
         if (lane == 0) mbar_arrive(&acc_empty);
         if (MODE == 1 && gm < a.Mvalid) {
-          // C -= product, 8 columns per batch of loads
+          // C -= product, 16 columns per batch of loads
 #pragma unroll
-          for (int c8 = 0; c8 < 6; ++c8) {
-            float2 cv[8];
+          for (int c16 = 0; c16 < OZ_EPI_COLS / 16; ++c16) {
+            float2 cv[16];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const int64_t gn = it.n0 + half * 48 + c8 * 8 + j;
+            for (int j = 0; j < 16; ++j) {
+              const int64_t gn = it.n0 + part * OZ_EPI_COLS + c16 * 16 + j;
               cv[j] = (gn < a.Nvalid) ? a.C[gn * a.ldc + gm] : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const int64_t gn = it.n0 + half * 48 + c8 * 8 + j;
+            for (int j = 0; j < 16; ++j) {
+              const int64_t gn = it.n0 + part * OZ_EPI_COLS + c16 * 16 + j;
               if (gn >= a.Nvalid) continue;
               const int64_t ci = gn * a.ldc + gm;
-              const f2 r = df_add({cv[j].x, cv[j].y}, {-acc[c8 * 8 + j].h, -acc[c8 * 8 + j].l});
+              const f2 r = df_add({cv[j].x, cv[j].y}, {-acc[c16 * 16 + j].h, -acc[c16 * 16 + j].l});
               if (gm < a.fp64_rows) a.C64[ci] = df_to_double(r);
               else a.C[ci] = make_float2(r.h, r.l);
             }
@@ -596,8 +673,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
       if (MODE == 0 && !s_fail && gm < a.AR) {
         float2* out = a.part + (int64_t)it.split * a.Nvalid * a.AR;
 #pragma unroll
-        for (int j = 0; j < 48; ++j) {
-          const int64_t gn = it.n0 + half * 48 + j;
+        for (int j = 0; j < OZ_EPI_COLS; ++j) {
+          const int64_t gn = it.n0 + part * OZ_EPI_COLS + j;
           if (gn < a.Nvalid) out[gn * a.AR + gm] = make_float2(acc[j].h, acc[j].l);
         }
       }
