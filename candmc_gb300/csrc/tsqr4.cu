@@ -409,6 +409,7 @@ struct Hr4Args {
   unsigned* done;   // pipelined tree: node finished (T, Q blocks, V written)
   unsigned* ticket; // pipelined tree: role counter
   int* fail;        // pipelined tree: a wait gave up
+  double* Pc;       // pipelined tree: prefix products of Q1_top along leaf 0's path, (depth + 1) x b x b
   int P;
   int ldS;          // leading dimension of the shared block (>= 32 * ceil(leaf rows / 32), >= 128)
   int depth;
@@ -433,25 +434,31 @@ __device__ void h4_root(const Hr4Args& a, double* sm) {
   double* sT = sY + b * b;
   __shared__ int s_sign[kDirectB];
   h4_load(sR, a.Rn + (size_t)a.base[a.depth] * b * b, b);
-  for (int idx = tid; idx < b * b; idx += blockDim.x) sM[idx] = (idx % b == idx / b) ? 1.0 : 0.0;
-  __syncthreads();
-  for (int lvl = a.depth; lvl >= 1; --lvl) {
-    if (h4_children(a, lvl, 0) > 1) {
-      h4_load(sX, a.Qn + ((size_t)a.base[lvl] * kFan + 0) * b * b, b);
-      h5_mm(sX, b, false, kSUpper, sM, b, false, kSUpper, sQ, b, b, 1.0, nullptr);
-      for (int idx = tid; idx < b * b; idx += blockDim.x) sM[idx] = sQ[idx];
-      __syncthreads();
+  if (a.Pc) {
+    // the pipelined tree multiplied Q1_top up leaf 0's path as its nodes finished
+    h4_load(sX, a.Pc + (size_t)a.depth * b * b, b);
+  } else {
+    // chain M = Q1^(1) ... Q1^(depth) of the first-child Q blocks (upper triangular)
+    for (int idx = tid; idx < b * b; idx += blockDim.x) sM[idx] = (idx % b == idx / b) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int lvl = a.depth; lvl >= 1; --lvl) {
+      if (h4_children(a, lvl, 0) > 1) {
+        h4_load(sX, a.Qn + ((size_t)a.base[lvl] * kFan + 0) * b * b, b);
+        h5_mm(sX, b, false, kSUpper, sM, b, false, kSUpper, sQ, b, b, 1.0, nullptr);
+        for (int idx = tid; idx < b * b; idx += blockDim.x) sM[idx] = sQ[idx];
+        __syncthreads();
+      }
     }
+    // Q1_top = C0 - V0 (T0 (V0^T C0)), V0 = unit-lower top block of leaf 0, C0 = M
+    for (int idx = tid; idx < b * b; idx += blockDim.x) {
+      const int r = idx % b, c = idx / b;
+      sY[idx] = (r > c) ? __ldcg(a.Vw + (int64_t)c * a.m + r) : (r == c ? 1.0 : 0.0);
+    }
+    h4_load(sT, a.Tl, b);
+    h5_mm(sY, b, true, kSUnitUpper, sM, b, false, kSUpper, sX, b, b, 1.0, nullptr);   // sX = V0^T C0 (upper)
+    h5_mm(sT, b, false, kSUpper, sX, b, false, kSUpper, sQ, b, b, 1.0, nullptr);      // sQ = T0 sX (upper)
+    h5_mm(sY, b, false, kSUnitLower, sQ, b, false, kSUpper, sX, b, b, -1.0, sM);      // sX = C0 - V0 sQ
   }
-  // Q1_top = C0 - V0 (T0 (V0^T C0)), V0 = unit-lower top block of leaf 0
-  for (int idx = tid; idx < b * b; idx += blockDim.x) {
-    const int r = idx % b, c = idx / b;
-    sY[idx] = (r > c) ? __ldcg(a.Vw + (int64_t)c * a.m + r) : (r == c ? 1.0 : 0.0);
-  }
-  h4_load(sT, a.Tl, b);
-  h5_mm(sY, b, true, kSUnitUpper, sM, b, false, kSUpper, sX, b, b, 1.0, nullptr);   // sX = V0^T C0
-  h5_mm(sT, b, false, kSUpper, sX, b, false, kSDense, sQ, b, b, 1.0, nullptr);      // sQ = T0 sX
-  h5_mm(sY, b, false, kSUnitLower, sQ, b, false, kSDense, sX, b, b, -1.0, sM);      // sX = C0 - V0 sQ
   double* sL = sX;   // Q1_top, becomes L\U
   __shared__ double s_rpiv;
   for (int i = 0; i < b; ++i) {
@@ -694,9 +701,20 @@ __device__ void h6_leaf(const Hr4Args& a, int leaf, double* sm, double* s_tau) {
   h4_tri_inv(G, b, false, Tt, scratch);
   double* Tleaf = a.Tl + (size_t)leaf * b * b;
   for (int idx = tid; idx < b * b; idx += blockDim.x) Tleaf[idx] = Tt[idx];
+  if (leaf == 0 && a.Pc) {
+    // P_0 = I - V0 T0 V0^T on the top b rows (V0 unit lower): the first factor
+    // of Q1_top, multiplied by the path nodes' Q1 blocks as they finish
+    h5_mm(Tt, b, false, kSUpper, S, ldS, true, kSUnitUpper, G, b, b, 1.0, nullptr);        // G = T0 V0^T
+    h5_mm(S, ldS, false, kSUnitLower, G, b, false, kSUpper, scratch, b, b, 1.0, nullptr);  // V0 G
+    for (int idx = tid; idx < b * b; idx += blockDim.x)
+      a.Pc[idx] = ((idx % b == idx / b) ? 1.0 : 0.0) - scratch[idx];
+  }
   __threadfence();
   __syncthreads();
-  if (tid == 0) st_release(a.done + leaf, 1u);
+  if (tid == 0) {
+    if (leaf == 0) st_release(a.prog + 0, (unsigned)b + 1u);
+    st_release(a.done + leaf, 1u);
+  }
 }
 
 __device__ void h6_node(const Hr4Args& a, int f, double* sm, double* s_tau, int* s_ok) {
@@ -714,6 +732,7 @@ __device__ void h6_node(const Hr4Args& a, int f, double* sm, double* s_tau, int*
   double* zv = Qk + b * b;
   double* wv = zv + 32;
   double* part = wv + 32;
+  double* Pb = part + 128;   // prefix product of Q1_top (nodes on leaf 0's path)
   for (int i = tid; i < ld * b; i += blockDim.x) S[i] = 0.0;
   for (int i = tid; i < b * b; i += blockDim.x) Tn[i] = 0.0;
   __syncthreads();
@@ -826,8 +845,30 @@ __device__ void h6_node(const Hr4Args& a, int f, double* sm, double* s_tau, int*
     if (tid == 0) Tn[j * b + j] = s_tau[j];
     __syncthreads();
   }
+  if (idx == 0) {
+    // on leaf 0's path: P_lvl = P_(lvl-1) Q1 = P_(lvl-1) (I - T), as soon as the
+    // child on the path has its prefix (it then sets its progress to b + 1).
+    // The root's solver waits for this node's prefix the same way.
+    if (tid == 0) *s_ok = h6_wait(a, a.prog + child0, (unsigned)b + 1u);
+    __syncthreads();
+    if (!*s_ok) {
+      h6_release_all(a, f);
+      return;
+    }
+    h4_load(Qk, a.Pc + (size_t)(lvl - 1) * b * b, b);
+    double* Pl = a.Pc + (size_t)lvl * b * b;
+    if (nch > 1) {
+      h5_mm(Qk, b, false, kSDense, Tn, b, false, kSUpper, Pb, b, b, -1.0, Qk);
+      for (int i = tid; i < b * b; i += blockDim.x) Pl[i] = Pb[i];
+    } else {
+      for (int i = tid; i < b * b; i += blockDim.x) Pl[i] = Qk[i];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release(a.prog + f, (unsigned)b + 1u);
+  }
   if (nch > 1) {
-    // Q blocks of the node: Q_1 = I - T;  Q_k = -V_k T
+    // Q blocks of the node (for forming Y): Q_1 = I - T;  Q_k = -V_k T
     double* Qp = a.Qn + (size_t)f * kFan * b * b;
     for (int i = tid; i < b * b; i += blockDim.x) {
       const int r = i % b, c = i / b;
@@ -842,19 +883,18 @@ __device__ void h6_node(const Hr4Args& a, int f, double* sm, double* s_tau, int*
   __threadfence();
   __syncthreads();
   if (tid == 0) st_release(a.done + f, 1u);
-  if (lvl == a.depth) {
-    // the root: the chain of leaf 0 (its T and V, the Q_1 blocks of its
-    // ancestors) must be complete
-    if (tid == 0) {
-      bool ok = h6_wait(a, a.done + 0, 1u);
-      for (int l = 1; l < a.depth && ok; ++l) ok = h6_wait(a, a.done + a.base[l], 1u);
-      *s_ok = ok;
-    }
-    __syncthreads();
-    if (!*s_ok) return;
-    __threadfence();
-    h4_root(a, sm);
-  }
+}
+
+// The root's solver (one extra CTA): once the top node has published its R
+// and the full prefix Q1_top, the sign-choice LU, T, W and U^-1, while the
+// top node still writes its Q blocks.
+__device__ void h6_root_solver(const Hr4Args& a, double* sm, int* s_ok) {
+  const int top = a.base[a.depth];
+  if (threadIdx.x == 0) *s_ok = h6_wait(a, a.prog + top, (unsigned)a.b + 1u);
+  __syncthreads();
+  if (!*s_ok) return;
+  __threadfence();
+  h4_root(a, sm);
 }
 
 __global__ void __launch_bounds__(kLeafThreads) k_hr6_pipe(Hr4Args a) {
@@ -863,11 +903,13 @@ __global__ void __launch_bounds__(kLeafThreads) k_hr6_pipe(Hr4Args a) {
   __shared__ int s_role, s_ok;
   if (threadIdx.x == 0) s_role = (int)atomicAdd(a.ticket, 1u);
   __syncthreads();
-  const int f = s_role;   // flat tree id: leaves 0 .. P-1, then the nodes level by level
+  const int f = s_role;   // flat tree id: leaves 0 .. P-1, the nodes level by level, the root's solver
   if (f < a.P)
     h6_leaf(a, f, sm6, s_tau);
-  else
+  else if (f <= a.base[a.depth])
     h6_node(a, f, sm6, s_tau, &s_ok);
+  else
+    h6_root_solver(a, sm6, &s_ok);
 }
 
 __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
@@ -901,7 +943,7 @@ __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
   }
   h4_load(sT, a.Tl + (size_t)leaf * b * b, b);
   h5_mm(sY, b, true, kSUnitUpper, sM, b, false, kSUpper, sX, b, b, 1.0, nullptr);   // sX = V_top^T M
-  h5_mm(sT, b, false, kSUpper, sX, b, false, kSDense, sY, b, b, 1.0, nullptr);      // sY = Z = T sX
+  h5_mm(sT, b, false, kSUpper, sX, b, false, kSUpper, sY, b, b, 1.0, nullptr);      // sY = Z = T sX
   for (int64_t r = r0 + tid; r < r1; r += blockDim.x) {
     if (r < b) continue;
     const int rl = (int)(r - r0);
@@ -958,7 +1000,7 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   // latency-bound panel); the level-by-level tree for many leaves, where the
   // leaves dominate and the pipeline would only add synchronisation
   const bool pipe = a.depth >= 1 && g_pipe_tree && nnodes <= 4096;
-  DevBuf vw, tl, rn, qn, cnt, uinv;
+  DevBuf vw, tl, rn, qn, cnt, uinv, pc;
   CANDMC_RET(vw.alloc(sizeof(double) * (size_t)m * b, s));
   CANDMC_RET(tl.alloc(sizeof(double) * nb2 * P, s));
   CANDMC_RET(rn.alloc(sizeof(double) * nb2 * nnodes, s));
@@ -967,6 +1009,7 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   const size_t ncnt = pipe ? 2 * (size_t)nnodes + 2 : (size_t)nnodes;
   CANDMC_RET(cnt.alloc(sizeof(unsigned) * ncnt, s));
   CANDMC_RET(uinv.alloc(sizeof(double) * nb2, s));
+  if (pipe) CANDMC_RET(pc.alloc(sizeof(double) * nb2 * (a.depth + 1), s));
   CANDMC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned) * ncnt, s));
   if (pipe) CANDMC_CK(cudaMemsetAsync(rn.p, 0, sizeof(double) * nb2 * nnodes, s));
   a.A = A; a.lda = lda; a.m = m; a.b = b;
@@ -977,6 +1020,7 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
     a.done = a.cnt + nnodes;
     a.ticket = a.cnt + 2 * nnodes;
     a.fail = reinterpret_cast<int*>(a.cnt + 2 * nnodes + 1);
+    a.Pc = pc.d();
   }
   a.T = T; a.ldT = ldT; a.W = W; a.ldW = ldW; a.Uinv = uinv.d(); a.status = d_status;
   static std::atomic<bool> attr{false};
@@ -989,7 +1033,7 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   {
     ProfScope ps(CANDMC_KCLASS_PANEL_LEAF, 2.0 * m * b * b, s);
     if (pipe)
-      k_hr6_pipe<<<(unsigned)nnodes, kLeafThreads, sm, s>>>(a);
+      k_hr6_pipe<<<(unsigned)nnodes + 1u, kLeafThreads, sm, s>>>(a);
     else
       k_hr4_leaf_tree<<<(unsigned)P, kLeafThreads, sm, s>>>(a);
   }
