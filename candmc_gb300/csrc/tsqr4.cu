@@ -120,6 +120,54 @@ __device__ __forceinline__ void warp_sum8(const double (&d)[8], double (&out)[8]
     out[k] = __shfl_sync(0xffffffffu, s, (((k >> 2) & 1) << 4) | (((k >> 1) & 1) << 3) | ((k & 1) << 2));
 }
 
+// The same reduction without the final broadcast: lane l returns sum number
+// 4 (l & 16 != 0) + 2 (l & 8 != 0) + (l & 4 != 0); the four lanes l with equal
+// bits 2..4 hold the same sum.
+__device__ __forceinline__ double warp_sum8_held(const double (&d)[8]) {
+  const int lane = threadIdx.x & 31;
+  const bool u16 = (lane & 16) != 0, u8 = (lane & 8) != 0, u4 = (lane & 4) != 0;
+  double p[4], q[2];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    p[k] = (u16 ? d[k + 4] : d[k]) + __shfl_xor_sync(0xffffffffu, u16 ? d[k] : d[k + 4], 16);
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    q[k] = (u8 ? p[k + 2] : p[k]) + __shfl_xor_sync(0xffffffffu, u8 ? p[k] : p[k + 2], 8);
+  double s = (u4 ? q[1] : q[0]) + __shfl_xor_sync(0xffffffffu, u4 ? q[0] : q[1], 4);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  return s;
+}
+
+__device__ __forceinline__ int warp_sum8_index(int lane) {
+  return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+}
+
+// Sixteen sums at once, without the broadcast: lane l returns sum number
+// 8 (l & 16 != 0) + 4 (l & 8 != 0) + 2 (l & 4 != 0) + (l & 2 != 0); lanes l and
+// l ^ 1 hold the same sum.
+__device__ __forceinline__ double warp_sum16_held(const double (&d)[16]) {
+  const int lane = threadIdx.x & 31;
+  const bool u16 = (lane & 16) != 0, u8 = (lane & 8) != 0, u4 = (lane & 4) != 0, u2 = (lane & 2) != 0;
+  double p[8], q[4], r[2];
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    p[k] = (u16 ? d[k + 8] : d[k]) + __shfl_xor_sync(0xffffffffu, u16 ? d[k] : d[k + 8], 16);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    q[k] = (u8 ? p[k + 4] : p[k]) + __shfl_xor_sync(0xffffffffu, u8 ? p[k] : p[k + 4], 8);
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    r[k] = (u4 ? q[k + 2] : q[k]) + __shfl_xor_sync(0xffffffffu, u4 ? q[k] : q[k + 2], 4);
+  double s = (u2 ? r[1] : r[0]) + __shfl_xor_sync(0xffffffffu, u2 ? r[0] : r[1], 2);
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  return s;
+}
+
+__device__ __forceinline__ int warp_sum16_index(int lane) {
+  return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+}
+
 // Reflector j from column j of S, by one warp: alpha = S[j][j], x = the tail
 // rows (lane l owns rows l + 32 t).  Writes beta to S[j][j],
 // v = x / (alpha - beta) to the tail rows, tau to s_tau[j] and v^T v / 2
@@ -731,18 +779,29 @@ __device__ void h6_node(const Hr4Args& a, int f, double* sm, double* s_tau, int*
   double* Qk = Tn + b * b;
   double* zv = Qk + b * b;
   double* wv = zv + 32;
-  double* part = wv + 32;
-  double* Pb = part + 128;   // prefix product of Q1_top (nodes on leaf 0's path)
+  double* yv = wv + 32;
+  double* part = yv + 32;    // 3 x 128 partial sums
+  double* Pb = part + 384;   // prefix product of Q1_top (nodes on leaf 0's path)
   for (int i = tid; i < ld * b; i += blockDim.x) S[i] = 0.0;
   for (int i = tid; i < b * b; i += blockDim.x) Tn[i] = 0.0;
   __syncthreads();
   auto tail = [](int r, int j) { return r >= 32 && (r & 31) <= j; };
+  // column c of R (head rows 0..c), published to the parent by warp 0
+  auto publish = [&](int c) {
+    if (lane <= c) Rme[c * b + lane] = S[c * ld + lane];
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) st_release(a.prog + f, (unsigned)(c + 1));
+  };
   for (int j = 0; j < b; ++j) {
-    // (1) column j of every child
-    if (tid == 0) {
+    // (1) column j of every child: lane k of warp 1 waits for child k, while
+    //     warp 0 publishes column j - 1 (finished in the last step)
+    if (warp == 0 && j > 0 && nch > 1) publish(j - 1);
+    if (warp == 1) {
       bool ok = true;
-      for (int k = 0; k < nch && ok; ++k) ok = h6_wait(a, a.prog + child0 + k, (unsigned)(j + 1));
-      *s_ok = ok;
+      if (lane < nch) ok = h6_wait(a, a.prog + child0 + lane, (unsigned)(j + 1));
+      ok = __all_sync(0xffffffffu, ok);
+      if (lane == 0) *s_ok = ok;
     }
     __syncthreads();
     if (!*s_ok) {
@@ -763,25 +822,49 @@ __device__ void h6_node(const Hr4Args& a, int f, double* sm, double* s_tau, int*
       S[j * ld + 32 * warp + lane] = __ldcg(a.Rn + (size_t)(child0 + warp) * b * b + j * b + lane);
     __syncthreads();
     if (j > 0) {
-      // (3) z_p = v_p^T s_j for p < j: head row p plus the children's rows
-      double dd[8], D[8];
+      // (3) one reduction for two sets of dot products over the children's
+      //     rows: z_p = v_p^T s_j (p < j; the head adds row p of s_j) and
+      //     y_p = v_p^T v_(j-1) (p < j - 1), which give column j - 1 of T
+      double dd[16];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        dd[q] = 0.0;
         const int pp = warp + 4 * q;
+        dd[q] = 0.0;
+        dd[8 + q] = 0.0;
         if (pp < j)
-          for (int k = 1; k < nch; ++k) dd[q] = fma(S[pp * ld + 32 * k + lane], S[j * ld + 32 * k + lane], dd[q]);
+          for (int k = 1; k < nch; ++k) {
+            const double vp = S[pp * ld + 32 * k + lane];
+            dd[q] = fma(vp, S[j * ld + 32 * k + lane], dd[q]);
+            if (pp < j - 1) dd[8 + q] = fma(vp, S[(j - 1) * ld + 32 * k + lane], dd[8 + q]);
+          }
       }
-      warp_sum8(dd, D);
-      if (lane == 0) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int pp = warp + 4 * q;
-          if (pp < j) zv[pp] = S[j * ld + pp] + D[q];
+      {
+        const double sq = warp_sum16_held(dd);
+        const int id = warp_sum16_index(lane);
+        const int pp = warp + 4 * (id & 7);
+        if ((lane & 1) == 0) {
+          if (id < 8) {
+            if (pp < j) zv[pp] = S[j * ld + pp] + sq;
+          } else if (pp < j - 1) {
+            yv[pp] = sq;
+          }
         }
       }
       __syncthreads();
-      // (4) w = T^T z
+      // (4) column c = j - 1 of T: T[p][c] = -tau_c sum_{q=p}^{c-1} T[p][q] y_q
+      const int c = j - 1;
+      if (c > 0) {
+        double acc = 0.0;
+        if (lane < c)
+          for (int q = warp; q < c; q += 4)
+            if (q >= lane) acc = fma(Tn[q * b + lane], yv[q], acc);
+        part[warp * 32 + lane] = acc;
+        __syncthreads();
+        if (warp == 0 && lane < c)
+          Tn[c * b + lane] = -s_tau[c] * ((part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]));
+        __syncthreads();
+      }
+      // (5) w = T^T z
       {
         double acc = 0.0;
         if (lane < j)
@@ -791,60 +874,65 @@ __device__ void h6_node(const Hr4Args& a, int f, double* sm, double* s_tau, int*
       __syncthreads();
       if (warp == 0 && lane < j) wv[lane] = (part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]);
       __syncthreads();
-      // (5) s_j -= V w: head rows p < j and the children's rows i < j
+      // (6) s_j -= V w: the head rows p < j directly; child k's rows r < j by
+      //     sum_{p<j} V_k[r][p] w_p (V_k[r][p] = 0 for r > p), p split over the warps
+      {
+        double acc[kFan - 1];
+#pragma unroll
+        for (int k = 0; k < kFan - 1; ++k) acc[k] = 0.0;
+        for (int pp = warp; pp < j; pp += 4) {
+          const double wp = wv[pp];
+#pragma unroll
+          for (int k = 1; k < kFan; ++k)
+            if (k < nch) acc[k - 1] = fma(S[pp * ld + 32 * k + lane], wp, acc[k - 1]);
+        }
+#pragma unroll
+        for (int k = 0; k < kFan - 1; ++k) part[k * 128 + warp * 32 + lane] = acc[k];
+      }
+      __syncthreads();
       if (warp == 0) {
         if (lane < j) S[j * ld + lane] -= wv[lane];
       } else if (warp < nch && lane < j) {
-        const int k = warp;
-        double acc = 0.0;
-        for (int pp = lane; pp < j; ++pp) acc = fma(S[pp * ld + 32 * k + lane], wv[pp], acc);
-        S[j * ld + 32 * k + lane] -= acc;
+        const double* pk = part + (warp - 1) * 128;
+        S[j * ld + 32 * warp + lane] -= (pk[lane] + pk[32 + lane]) + (pk[64 + lane] + pk[96 + lane]);
       }
       __syncthreads();
     }
-    // (6) reflector j, then publish column j of R
-    if (warp == 0) {
-      h5_reflector<kFan>(S, ld, nch * 32, j, b, tail, s_tau, Qk);
-      __syncwarp();
-      if (lane <= j) Rme[j * b + lane] = S[j * ld + lane];
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) st_release(a.prog + f, (unsigned)(j + 1));
-    }
+    // (7) reflector j; T[j][j] = tau_j (read from the next step on)
+    if (warp == 0) h5_reflector<kFan>(S, ld, nch * 32, j, b, tail, s_tau, Qk);
     __syncthreads();
-    // (7) column j of T: T[p][j] = -tau_j sum_{q=p}^{j-1} T[p][q] (v_q^T v_j)
-    if (j > 0) {
-      double dd[8], D[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        dd[q] = 0.0;
-        const int pp = warp + 4 * q;
-        if (pp < j)
-          for (int k = 1; k < nch; ++k) dd[q] = fma(S[pp * ld + 32 * k + lane], S[j * ld + 32 * k + lane], dd[q]);
-      }
-      warp_sum8(dd, D);
-      if (lane == 0) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int pp = warp + 4 * q;
-          if (pp < j) zv[pp] = D[q];
-        }
-      }
-      __syncthreads();
-      {
-        double acc = 0.0;
-        if (lane < j)
-          for (int q = warp; q < j; q += 4)
-            if (q >= lane) acc = fma(Tn[q * b + lane], zv[q], acc);
-        part[warp * 32 + lane] = acc;
-      }
-      __syncthreads();
-      if (warp == 0 && lane < j)
-        Tn[j * b + lane] = -s_tau[j] * ((part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]));
-    }
     if (tid == 0) Tn[j * b + j] = s_tau[j];
-    __syncthreads();
   }
+  if (nch > 1 && b > 1) {
+    // the last column of T: y_p = v_p^T v_(b-1), p < b - 1
+    const int c = b - 1;
+    double dd[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      dd[q] = 0.0;
+      const int pp = warp + 4 * q;
+      if (pp < c)
+        for (int k = 1; k < nch; ++k) dd[q] = fma(S[pp * ld + 32 * k + lane], S[c * ld + 32 * k + lane], dd[q]);
+    }
+    {
+      const double sq = warp_sum8_held(dd);
+      const int pp = warp + 4 * warp_sum8_index(lane);
+      if ((lane & 3) == 0 && pp < c) yv[pp] = sq;
+    }
+    __syncthreads();
+    {
+      double acc = 0.0;
+      if (lane < c)
+        for (int q = warp; q < c; q += 4)
+          if (q >= lane) acc = fma(Tn[q * b + lane], yv[q], acc);
+      part[warp * 32 + lane] = acc;
+    }
+    __syncthreads();
+    if (warp == 0 && lane < c)
+      Tn[c * b + lane] = -s_tau[c] * ((part[lane] + part[32 + lane]) + (part[64 + lane] + part[96 + lane]));
+  }
+  __syncthreads();
+  if (nch > 1 && warp == 0) publish(b - 1);
   if (idx == 0) {
     // on leaf 0's path: P_lvl = P_(lvl-1) Q1 = P_(lvl-1) (I - T), as soon as the
     // child on the path has its prefix (it then sets its progress to b + 1).
