@@ -365,6 +365,7 @@ __device__ void h5_mm(const double* A, int lda, bool at, int as, const double* B
       if ((p++ % nwarp) != warp) continue;
       const int i = i0 + (lane & 7), jA = j0 + (lane >> 3), jB = jA + 4;
       double acc0 = 0.0, acc1 = 0.0;
+#pragma unroll 4
       for (int k = klo; k <= khi; ++k) {
         const double a = (i < b) ? h5_at(A, lda, at, as, i, k) : 0.0;
         const double b0 = (jA < b) ? h5_at(B, ldb, bt, bs, k, jA) : 0.0;
@@ -435,6 +436,22 @@ __device__ void h4_tri_inv(const double* X, int b, bool unit, double* Xi, double
 __device__ void h4_load(double* dst, const double* src, int b) {
   for (int idx = threadIdx.x; idx < b * b; idx += blockDim.x) dst[idx] = __ldcg(src + idx);
   __syncthreads();
+}
+
+// Rows [0, L) of b columns of a column-major block (ld lda) into S (ld ldS),
+// zero below row L: sixteen columns' loads in flight per thread before any
+// store, so the block costs two memory latencies rather than b.
+__device__ void h4_load_block(double* S, int ldS, const double* A, int64_t lda, int L, int b) {
+  for (int r = threadIdx.x; r < ldS; r += blockDim.x) {
+    for (int c0 = 0; c0 < b; c0 += 16) {
+      double t[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) t[u] = (r < L && c0 + u < b) ? A[(int64_t)(c0 + u) * lda + r] : 0.0;
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        if (c0 + u < b) S[(c0 + u) * ldS + r] = t[u];
+    }
+  }
 }
 
 struct Hr4Args {
@@ -509,22 +526,37 @@ __device__ void h4_root(const Hr4Args& a, double* sm) {
   }
   double* sL = sX;   // Q1_top, becomes L\U
   __shared__ double s_rpiv;
-  for (int i = 0; i < b; ++i) {
-    if (tid == 0) {
-      const double d = sL[i * b + i];
-      const int s = d > 0.0 ? -1 : 1;
-      s_sign[i] = s;
-      sL[i * b + i] = d - (double)s;
-      s_rpiv = nr_rcp(d - (double)s);   // |d - s| >= 1: the sign choice keeps the pivot away from 0
+  // Sign-choice LU without pivoting, with a one-column lookahead: in step i,
+  // warp 0 applies column i to column i + 1 and finishes it (pivot, sign,
+  // multipliers) while the other warps apply column i to the columns beyond;
+  // one barrier per column.
+  const int warp = tid >> 5, lane = tid & 31;
+  auto pivot = [&](int c) {   // warp 0: the diagonal of column c, then its multipliers
+    if (lane == 0) {
+      const double d = sL[c * b + c];
+      const int sg = d > 0.0 ? -1 : 1;
+      s_sign[c] = sg;
+      sL[c * b + c] = d - (double)sg;
+      s_rpiv = nr_rcp(d - (double)sg);   // |d - s| >= 1: the sign choice keeps the pivot away from 0
     }
-    __syncthreads();
-    const double rpiv = s_rpiv;
-    for (int r = i + 1 + tid; r < b; r += blockDim.x) sL[i * b + r] *= rpiv;
-    __syncthreads();
-    const int n = b - i - 1;
-    for (int idx = tid; idx < n * n; idx += blockDim.x) {
-      const int r = i + 1 + idx % n, c = i + 1 + idx / n;
-      sL[c * b + r] = fma(-sL[i * b + r], sL[c * b + i], sL[c * b + r]);
+    __syncwarp();
+    const double rp = s_rpiv;
+    for (int r = c + 1 + lane; r < b; r += 32) sL[c * b + r] *= rp;
+  };
+  if (warp == 0) pivot(0);
+  __syncthreads();
+  for (int i = 0; i + 1 < b; ++i) {
+    const int c1 = i + 1;
+    if (warp == 0) {
+      for (int r = c1 + lane; r < b; r += 32) sL[c1 * b + r] = fma(-sL[i * b + r], sL[c1 * b + i], sL[c1 * b + r]);
+      __syncwarp();
+      pivot(c1);
+    } else {
+      const int n = b - c1, nc = b - c1 - 1;   // rows i + 1 .., columns i + 2 ..
+      for (int idx = tid - 32; idx < n * nc; idx += blockDim.x - 32) {
+        const int r = c1 + idx % n, c = c1 + 1 + idx / n;
+        sL[c * b + r] = fma(-sL[i * b + r], sL[c * b + i], sL[c * b + r]);
+      }
     }
     __syncthreads();
   }
@@ -573,8 +605,7 @@ __global__ void __launch_bounds__(kLeafThreads) k_hr4_leaf_tree(Hr4Args a) {
   double* scratch = Tt + b * b;
 
   // ---- leaf: Householder QR of rows [r0, r0 + L); rows L..ldS-1 are zero
-  for (int c = 0; c < b; ++c)
-    for (int r = tid; r < ldS; r += blockDim.x) S[c * ldS + r] = (r < L) ? a.A[c * a.lda + r0 + r] : 0.0;
+  h4_load_block(S, ldS, a.A + r0, a.lda, L, b);
   for (int idx = tid; idx < b * b; idx += blockDim.x) G[idx] = 0.0;
   __syncthreads();
   {
@@ -730,8 +761,7 @@ __device__ void h6_leaf(const Hr4Args& a, int leaf, double* sm, double* s_tau) {
   double* G = S + (size_t)ldS * b;
   double* Tt = G + b * b;
   double* scratch = Tt + b * b;
-  for (int c = 0; c < b; ++c)
-    for (int r = tid; r < ldS; r += blockDim.x) S[c * ldS + r] = (r < L) ? a.A[c * a.lda + r0 + r] : 0.0;
+  h4_load_block(S, ldS, a.A + r0, a.lda, L, b);
   for (int idx = tid; idx < b * b; idx += blockDim.x) G[idx] = 0.0;
   __syncthreads();
   const LeafPublish pub{a.Rn + (size_t)leaf * b * b, b, a.prog + leaf};
@@ -1032,6 +1062,9 @@ __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
   h4_load(sT, a.Tl + (size_t)leaf * b * b, b);
   h5_mm(sY, b, true, kSUnitUpper, sM, b, false, kSUpper, sX, b, b, 1.0, nullptr);   // sX = V_top^T M
   h5_mm(sT, b, false, kSUpper, sX, b, false, kSUpper, sY, b, b, 1.0, nullptr);      // sY = Z = T sX
+  // Z is upper triangular: Y[r][c] = M[r][c] - sum_{k<=c} V[r][k] Z[k][c], eight
+  // columns at a time with independent accumulators (the loops unroll fully,
+  // so the triangle is cut at compile time)
   for (int64_t r = r0 + tid; r < r1; r += blockDim.x) {
     if (r < b) continue;
     const int rl = (int)(r - r0);
@@ -1039,12 +1072,25 @@ __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
 #pragma unroll
     for (int k = 0; k < kDirectB; ++k)
       v[k] = (k < b) ? (rl > k ? a.Vw[(int64_t)k * a.m + r] : (rl == k ? 1.0 : 0.0)) : 0.0;
-    for (int c = 0; c < b; ++c) {
-      double acc = (rl < b) ? sM[c * b + rl] : 0.0;
 #pragma unroll
-      for (int k = 0; k < kDirectB; ++k)
-        if (k < b) acc = fma(-v[k], sY[c * b + k], acc);
-      a.A[c * a.lda + r] = acc;
+    for (int cb = 0; cb < kDirectB; cb += 8) {
+      if (cb < b) {
+        double acc[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[u] = (rl < b && cb + u < b) ? sM[(cb + u) * b + rl] : 0.0;
+#pragma unroll
+        for (int k = 0; k < cb + 8; ++k) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (k <= cb + u) {
+              const double z = (cb + u < b) ? sY[(cb + u) * b + k] : 0.0;
+              acc[u] = fma(-v[k], z, acc[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (cb + u < b) a.A[(int64_t)(cb + u) * a.lda + r] = acc[u];
+      }
     }
   }
 }
@@ -1088,29 +1134,40 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   // latency-bound panel); the level-by-level tree for many leaves, where the
   // leaves dominate and the pipeline would only add synchronisation
   const bool pipe = a.depth >= 1 && g_pipe_tree && nnodes <= 4096;
-  DevBuf vw, tl, rn, qn, cnt, uinv, pc;
-  CANDMC_RET(vw.alloc(sizeof(double) * (size_t)m * b, s));
-  CANDMC_RET(tl.alloc(sizeof(double) * nb2 * P, s));
-  CANDMC_RET(rn.alloc(sizeof(double) * nb2 * nnodes, s));
-  CANDMC_RET(qn.alloc(sizeof(double) * nb2 * kFan * nnodes, s));
+  // one workspace, carved in 256-byte aligned pieces; the counters and the
+  // node R blocks (read before all their entries are written) lead it, so
+  // one memset clears both
   // counters: cnt (last arriver) or prog + done + ticket + fail (pipelined)
   const size_t ncnt = pipe ? 2 * (size_t)nnodes + 2 : (size_t)nnodes;
-  CANDMC_RET(cnt.alloc(sizeof(unsigned) * ncnt, s));
-  CANDMC_RET(uinv.alloc(sizeof(double) * nb2, s));
-  if (pipe) CANDMC_RET(pc.alloc(sizeof(double) * nb2 * (a.depth + 1), s));
-  CANDMC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned) * ncnt, s));
-  if (pipe) CANDMC_CK(cudaMemsetAsync(rn.p, 0, sizeof(double) * nb2 * nnodes, s));
+  auto rup256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_cnt = 0;
+  const size_t o_rn = o_cnt + rup256(sizeof(unsigned) * ncnt);
+  const size_t o_vw = o_rn + rup256(sizeof(double) * nb2 * nnodes);
+  const size_t o_tl = o_vw + rup256(sizeof(double) * (size_t)m * b);
+  const size_t o_qn = o_tl + rup256(sizeof(double) * nb2 * P);
+  const size_t o_uinv = o_qn + rup256(sizeof(double) * nb2 * kFan * nnodes);
+  const size_t o_pc = o_uinv + rup256(sizeof(double) * nb2);
+  const size_t total_bytes = o_pc + (pipe ? rup256(sizeof(double) * nb2 * (a.depth + 1)) : 0);
+  DevBuf ws;
+  CANDMC_RET(ws.alloc(total_bytes, s));
+  char* base = static_cast<char*>(ws.p);
+  CANDMC_CK(cudaMemsetAsync(base, 0, pipe ? o_vw : o_rn, s));
   a.A = A; a.lda = lda; a.m = m; a.b = b;
-  a.Vw = vw.d(); a.Tl = tl.d(); a.Rn = rn.d(); a.Qn = qn.d();
-  a.cnt = static_cast<unsigned*>(cnt.p);
+  a.Vw = reinterpret_cast<double*>(base + o_vw);
+  a.Tl = reinterpret_cast<double*>(base + o_tl);
+  a.Rn = reinterpret_cast<double*>(base + o_rn);
+  a.Qn = reinterpret_cast<double*>(base + o_qn);
+  a.cnt = reinterpret_cast<unsigned*>(base + o_cnt);
   if (pipe) {
     a.prog = a.cnt;
     a.done = a.cnt + nnodes;
     a.ticket = a.cnt + 2 * nnodes;
     a.fail = reinterpret_cast<int*>(a.cnt + 2 * nnodes + 1);
-    a.Pc = pc.d();
+    a.Pc = reinterpret_cast<double*>(base + o_pc);
   }
-  a.T = T; a.ldT = ldT; a.W = W; a.ldW = ldW; a.Uinv = uinv.d(); a.status = d_status;
+  a.T = T; a.ldT = ldT; a.W = W; a.ldW = ldW;
+  a.Uinv = reinterpret_cast<double*>(base + o_uinv);
+  a.status = d_status;
   static std::atomic<bool> attr{false};
   if (!attr) {
     CANDMC_CK(cudaFuncSetAttribute(k_hr4_leaf_tree, cudaFuncAttributeMaxDynamicSharedMemorySize,
