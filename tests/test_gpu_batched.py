@@ -2,7 +2,7 @@
 optional CUDA-graph replay) against the least-squares oracle / LAPACK.
 
 Tolerance: x_i within 1e-12 relative of LAPACK's lstsq for these
-well-conditioned Gaussian problems (the benchmark spec's 1e-12 bar)."""
+well-conditioned Gaussian problems (the FP64-class 1e-12 bar)."""
 import numpy as np
 import pytest
 

@@ -1,7 +1,7 @@
 """FP32 form of the trailing update and the least-squares solver with FP64
 iterative refinement.
 
-Tolerances (the benchmark spec's): refined least-squares solutions within 1e-12
+Tolerances: refined least-squares solutions within 1e-12
 relative of the FP64 oracle for well-conditioned problems; the FP32-form
 factorization itself is FP32-accurate (backward error FP32_BWD_TOL).  For
 ill-conditioned problems forward agreement is limited by kappa * u, so the

@@ -1,6 +1,6 @@
 """Emulated-FP64 form (BF16 Ozaki slices on tcgen05, FP32 accumulation).
 
-Tolerance stated by the north star for the FP64 and emulated-FP64 forms:
+Tolerance for the FP64 and emulated-FP64 forms (FP64-class results):
 backward error ||A - QR||_F / ||A||_F <= 1e-13.  Element-wise, the emulated
 trailing update agrees with the FP64 update to EMU_TOL relative to the
 largest entry (a few FP64 ulps times the contraction length).
