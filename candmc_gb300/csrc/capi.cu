@@ -35,7 +35,7 @@ int cuda_status(cudaError_t e, const char* where) {
 }
 
 // Once per device: keep freed stream-ordered scratch in the device's default
-// pool instead of returning it to the driver at every synchronisation, so a
+// pool instead of returning it to the CUDA driver at every synchronisation, so a
 // repeated factorization reuses its scratch without re-mapping memory.
 static void ensure_pool() {
   static std::atomic<bool> done[64] = {};

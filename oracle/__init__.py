@@ -1,4 +1,4 @@
-"""Oracle for the CANDMC QR hot path: a CPU restatement used only as the checker.
+"""Oracle for the CANDMC QR hot path: a CPU restatement, the reference the tests check against.
 
 TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the CPU
 baseline leg of bench.py may import this package; the product library never

@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module; the
 tests, the smoke check and the CPU-baseline leg of the benchmark use it as
-the checker.
+the reference result.
 
 Each function restates one reference function (paths relative to the CANDMC
 source tree) on numpy float64 arrays, with the LAPACK arithmetic from
