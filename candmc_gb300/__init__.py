@@ -1,7 +1,8 @@
 """GB300-native QR hot path of CANDMC: TSQR, Householder reconstruction, CAQR.
 
 Python mirror of the reference's QR entry points (include/CANDMC.h ->
-alg/QR/tsqr/bitree_tsqr.h, alg/QR/hh_recon/hh_recon.h, alg/QR/qr_2d/qr_2d.h)
+alg/QR/tsqr/bitree_tsqr.h, alg/QR/hh_recon/hh_recon.h, alg/QR/qr_2d/qr_2d.h,
+alg/QR/qr_2d/qr_y2d.h)
 on one GPU: the process grid is 1 x 1, so the MPI arguments (myRank, numPes,
 root, req_id, CommData_t, pview) disappear.  Every function calls the C ABI
 of libcandmc_gb300.so (include/candmc_gb300.h); there is no CPU fallback and
@@ -15,6 +16,8 @@ Matrices are column-major float64, as in the reference:
     reference's pointers are host memory).
 Errors raise CandmcError (the reference asserts/aborts instead).
 """
+import ctypes
+
 import numpy as np
 
 from . import _abi
@@ -23,7 +26,8 @@ from ._abi import CandmcError, check
 __all__ = [
     "CandmcError", "colmajor", "empty_colmajor", "hh_recon_qr", "bitree_tsqr", "construct_Q1",
     "compute_invT_from_W", "signed_NLU", "recursive_NLU", "compute_invT_from_Y",
-    "compute_invT_from_Y2", "upd_A", "update_A", "QR_2D", "QR_2D_2D", "QR_2D_pipe", "ls_solve",
+    "compute_invT_from_Y2", "upd_A", "update_A", "QR_2D", "QR_2D_2D", "QR_2D_pipe", "Yamamoto",
+    "upd_Yamamoto_A", "Aggregator", "QR_Yamamoto_2D", "QR_Yamamoto_2D_2D", "ls_solve",
     "batched_ls", "batched_status", "set_tuning", "PRECISIONS", "lib",
 ]
 
@@ -286,6 +290,99 @@ def QR_2D_2D(A, b, b_sub, aggreg_Y=None, precision="fp64", stream=None):
     pg, ldg = _dev(aggreg_Y, "aggreg_Y") if aggreg_Y is not None else (None, 0)
     check(lib().candmc_QR_2D_2D(pa, lda, m, k, b, b_sub, pg, ldg, _prec(precision), _stream(stream)),
           "QR_2D_2D")
+    return A
+
+
+def Yamamoto(A, Qm=None, W=None, stream=None):
+    """TSQR and Yamamoto's basis-kernel representation of an m x b panel
+    (alg/QR/hh_recon/yamamoto.h:21-32).
+
+    A becomes Y\\(S*R).  Returns (Qm, W) with Q^T = I + Qm W Qm^T; the pair
+    equals the reference's up to the reference's own column signs (see
+    candmc_Yamamoto in include/candmc_gb300.h).
+    """
+    m, b = A.shape
+    Qm = empty_colmajor(m, b, A.device) if Qm is None else Qm
+    W = empty_colmajor(b, b, A.device) if W is None else W
+    pa, lda = _dev(A, "A")
+    pq, ldq = _dev(Qm, "Qm")
+    check(lib().candmc_Yamamoto(pa, lda, pq, ldq, m, b, _dev(W, "W")[0], _stream(stream)), "Yamamoto")
+    return Qm, W
+
+
+def upd_Yamamoto_A(Qm, A, W, precision="fp64", stream=None):
+    """A += Qm (W (Qm^T A)) (alg/QR/qr_2d/qr_y2d.h:79-99)."""
+    mb, b = Qm.shape
+    kb = A.shape[1]
+    pq, ldq = _dev(Qm, "Qm")
+    pa, lda = _dev(A, "A")
+    check(lib().candmc_upd_Yamamoto_A(pq, ldq, pa, lda, mb, kb, b, _dev(W, "W")[0], _prec(precision),
+                                      _stream(stream)), "upd_Yamamoto_A")
+    return A
+
+
+class Aggregator:
+    """The reference's aggregator (alg/QR/qr_2d/qr_y2d.h:4-44) on the device:
+    aQm (lda_aQm x lda_aT) and the block-lower aT (lda_aT x lda_aT), zeroed."""
+
+    def __init__(self, lda_aQm, lda_aT, device="cuda"):
+        torch = _torch()
+        self.lda_aQm, self.lda_aT = lda_aQm, lda_aT
+        self.aQm = colmajor(torch.zeros(lda_aQm, lda_aT, dtype=torch.float64, device=device))
+        self.aT = colmajor(torch.zeros(lda_aT, lda_aT, dtype=torch.float64, device=device))
+        self.n = 0
+        self.shift = 0
+
+    def reset(self):
+        self.aQm.zero_()
+        self.aT.zero_()
+        self.n = 0
+        self.shift = 0
+
+    def shift_down(self, b):
+        self.shift += b
+
+    def append(self, Qm, T, stream=None):
+        mb, b = Qm.shape
+        pq, ldq = _dev(Qm, "Qm")
+        check(lib().candmc_yamamoto_append(self.aQm.data_ptr(), self.lda_aQm, self.aT.data_ptr(), self.lda_aT,
+                                           self.n, self.shift, mb, b, pq, ldq, _dev(T, "T")[0],
+                                           _stream(stream)), "aggregator append")
+        self.n += b
+
+    def _args(self):
+        n, sh = ctypes.c_int64(self.n), ctypes.c_int64(self.shift)
+        return n, sh, (self.aQm.data_ptr(), self.lda_aQm, self.aT.data_ptr(), self.lda_aT,
+                       ctypes.byref(n), ctypes.byref(sh))
+
+
+def QR_Yamamoto_2D(A, b, agg=None, compute_Y=False, precision="fp64", stream=None):
+    """CAQR with Yamamoto's representation (alg/QR/qr_2d/qr_y2d.h:102-119)."""
+    m, k = A.shape
+    pa, lda = _dev(A, "A")
+    if agg is None:
+        rest = (None, 0, None, 0, None, None)
+    else:
+        n, sh, rest = agg._args()
+    check(lib().candmc_QR_Yamamoto_2D(pa, lda, m, k, b, int(bool(compute_Y)), *rest, _prec(precision),
+                                      _stream(stream)), "QR_Yamamoto_2D")
+    if agg is not None:
+        agg.n, agg.shift = n.value, sh.value
+    return A
+
+
+def QR_Yamamoto_2D_2D(A, b, b_sub, agg=None, compute_Y=False, precision="fp64", stream=None):
+    """Two-level blocked CAQR with Yamamoto's representation (alg/QR/qr_2d/qr_y2d.h:122-139)."""
+    m, k = A.shape
+    pa, lda = _dev(A, "A")
+    if agg is None:
+        rest = (None, 0, None, 0, None, None)
+    else:
+        n, sh, rest = agg._args()
+    check(lib().candmc_QR_Yamamoto_2D_2D(pa, lda, m, k, b, b_sub, int(bool(compute_Y)), *rest,
+                                         _prec(precision), _stream(stream)), "QR_Yamamoto_2D_2D")
+    if agg is not None:
+        agg.n, agg.shift = n.value, sh.value
     return A
 
 

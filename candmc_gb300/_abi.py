@@ -13,6 +13,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "candmc_gb300.h")
 _i64 = ctypes.c_int64
 _int = ctypes.c_int
 _vp = ctypes.c_void_p
+_pi64 = ctypes.POINTER(ctypes.c_int64)
 
 # name -> argtypes (restype int unless listed in _RESTYPES)
 SIGNATURES = {
@@ -35,6 +36,13 @@ SIGNATURES = {
     "candmc_QR_2D": [_vp, _i64, _i64, _i64, _i64, _vp, _i64, _int, _vp],
     "candmc_QR_2D_host": [_vp, _i64, _i64, _i64, _i64, _int],
     "candmc_QR_2D_2D": [_vp, _i64, _i64, _i64, _i64, _i64, _vp, _i64, _int, _vp],
+    "candmc_Yamamoto": [_vp, _i64, _vp, _i64, _i64, _i64, _vp, _vp],
+    "candmc_upd_Yamamoto_A": [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _int, _vp],
+    "candmc_yamamoto_append": [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _i64, _vp, _i64, _vp, _vp],
+    "candmc_QR_Yamamoto_2D": [_vp, _i64, _i64, _i64, _i64, _int, _vp, _i64, _vp, _i64, _pi64, _pi64, _int,
+                              _vp],
+    "candmc_QR_Yamamoto_2D_2D": [_vp, _i64, _i64, _i64, _i64, _i64, _int, _vp, _i64, _vp, _i64, _pi64, _pi64,
+                                 _int, _vp],
     "candmc_QR_2D_pipe": [_vp, _i64, _i64, _i64, _i64, _int, _vp],
     "candmc_ls_solve": [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int, _int,
                         ctypes.c_double, _vp, _vp],

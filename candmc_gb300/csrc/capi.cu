@@ -412,6 +412,177 @@ struct HostMat {
   }
 };
 
+
+// ------------------------------------------------------- Yamamoto's representation
+// Yamamoto's basis-kernel representation (alg/QR/hh_recon/yamamoto.cxx,
+// alg/QR/qr_2d/qr_y2d.cxx): Q_HH^T = I + Qm W Qm^T with Qm = [Q1 - S; Q2] and
+// W = (Q1 - S)^-1 S for the first b columns [Q1; Q2] of a TSQR basis.  From
+// the Householder reconstruction of the panel (Y unit lower in A, W_hr = U S)
+// the basis [Q1; Q2] S satisfies Q1 S - I = L W_hr, which gives
+//   Qm = Y W_hr,  W = W_hr^-1 L^-1  (and S = I for that basis).
+// These equal the reference's pair up to its own sign matrix S_ref
+// (Qm_ref = Qm S_ref, W_ref = S_ref W S_ref); the products the
+// representation is used for (Qm W Qm^T, the updates, S R) are the same.
+struct YAgg {
+  double* aQm;
+  int64_t ld_aqm;   // rows of aQm
+  double* aT;
+  int64_t ld_at;    // rows of aT, columns of aQm and aT
+  int64_t n;
+  int64_t shift;
+};
+
+static int yamamoto_from_hr(const double* A, int64_t lda, int64_t m, int64_t b, const double* whr,
+                            double* Qm, int64_t ldq, double* W, cudaStream_t s) {
+  DevBuf tmp;
+  CANDMC_RET(tmp.alloc(sizeof(double) * 3 * b * b, s));
+  double* eye = tmp.d();
+  double* negw = eye + b * b;
+  double* li = negw + b * b;
+  // Qm = Y W_hr, as Qm (zeroed) -= Y (-W_hr)
+  CANDMC_RET(set_identity(eye, b, b, b, s));
+  CANDMC_RET(small_gemm(b, b, b, -1.0, mref(eye, b), mref(whr, b, 0, kUpper), 0.0, negw, b, s));
+  CANDMC_CK(cudaMemset2DAsync(Qm, sizeof(double) * ldq, 0, sizeof(double) * m, b, s));
+  CANDMC_RET(gemm_nn_sub(Qm, ldq, mref(A, lda, 0, kUnitLower), negw, b, m, b, (int)b, s));
+  // W = W_hr^-1 L^-1
+  CANDMC_RET(tri_inv(whr, b, (int)b, 0, 0, eye, b, s));
+  CANDMC_RET(tri_inv(A, lda, (int)b, 1, 1, li, b, s));
+  CANDMC_RET(small_gemm(b, b, b, 1.0, mref(eye, b, 0, kUpper), mref(li, b, 0, kLower), 0.0, W, b, s));
+  return CANDMC_OK;
+}
+
+// Yamamoto on one panel (yamamoto.cxx:98-174): A becomes Y\(S R), Qm (ldq) and
+// W (b x b, ld b) the representation.
+static int yamamoto_panel(double* A, int64_t lda, int64_t m, int64_t b, double* Qm, int64_t ldq,
+                          double* W, int* st, cudaStream_t s) {
+  DevBuf whr, t;
+  CANDMC_RET(whr.alloc(sizeof(double) * b * b, s));
+  CANDMC_RET(t.alloc(sizeof(double) * b * b, s));
+  CANDMC_RET(hh_recon_dev(A, lda, m, b, whr.d(), b, t.d(), b, st, CANDMC_PREC_FP64, s));
+  return yamamoto_from_hr(A, lda, m, b, whr.d(), Qm, ldq, W, s);
+}
+
+// A (mb x kb) += Qm (W (Qm^T A)) in the requested arithmetic (qr_y2d.cxx:133-178).
+static int upd_yamamoto(const double* Qm, int64_t ldq, double* A, int64_t lda, int64_t mb, int64_t kb,
+                        int64_t b, const double* W, int64_t ldw, int precision, cudaStream_t s) {
+  if (mb <= 0 || kb <= 0) return CANDMC_OK;
+  if (precision == CANDMC_PREC_FP64) {
+    DevBuf z;
+    CANDMC_RET(z.alloc(sizeof(double) * b * kb, s));
+    CANDMC_RET(gemm_tn_reduce(mref(Qm, ldq), mref(A, lda), mb, (int)b, kb, mref(W, ldw), -1.0, z.d(),
+                              b, s));
+    return gemm_nn_sub(A, lda, mref(Qm, ldq), z.d(), b, mb, kb, (int)b, s);
+  }
+  if (precision != CANDMC_PREC_OZAKI && precision != CANDMC_PREC_FP32)
+    return set_error(CANDMC_ERR_ARG, "unknown precision form");
+  if (b > 128) return set_error(CANDMC_ERR_ARG, "the ozaki and fp32 forms need b <= 128");
+  // the emulated contractions apply A -= Qm Top (Qm^T A): Top = -W
+  DevBuf nw;
+  CANDMC_RET(nw.alloc(sizeof(double) * 2 * b * b, s));
+  CANDMC_RET(set_identity(nw.d() + b * b, b, b, b, s));
+  CANDMC_RET(small_gemm(b, b, b, -1.0, mref(W, ldw), mref(nw.d() + b * b, b), 0.0, nw.d(), b, s));
+  Status st;
+  CANDMC_RET(st.init(s));
+  CANDMC_RET(to_df64(A, lda, mb, kb, s));
+  if (precision == CANDMC_PREC_OZAKI)
+    CANDMC_RET(apply_qt_ozaki(Qm, ldq, kDense, mb, (int)b, mref(nw.d(), b), A, lda, kb, 0, st.p(), s));
+  else
+    CANDMC_RET(apply_qt_f32(Qm, ldq, kDense, mb, (int)b, mref(nw.d(), b), A, lda, kb, 0, s));
+  return from_df64(A, lda, mb, kb, s);
+}
+
+// aggregator::append (qr_y2d.cxx:38-66): Qm below the previous panels, and
+// the new block row of the block-lower aT: [T (Qm^T aQm) aT, T].
+static int yamamoto_append(YAgg* g, int64_t mb, int64_t b, const double* Qm, int64_t ldq, const double* T,
+                           int64_t ldt, cudaStream_t s) {
+  const int64_t n = g->n, sh = g->shift;
+  if (n + b > g->ld_at || (mb > 0 && sh + mb > g->ld_aqm))
+    return set_error(CANDMC_ERR_ARG, "aggregator too small for the appended panel");
+  if (mb > 0)
+    CANDMC_CK(cudaMemcpy2DAsync(g->aQm + n * g->ld_aqm + sh, sizeof(double) * g->ld_aqm, Qm,
+                                sizeof(double) * ldq, sizeof(double) * mb, b, cudaMemcpyDeviceToDevice, s));
+  if (n > 0) {
+    DevBuf x;
+    CANDMC_RET(x.alloc(sizeof(double) * 2 * b * n, s));
+    if (mb > 0)
+      CANDMC_RET(gemm_tn_reduce(mref(Qm, ldq), mref(g->aQm + sh, g->ld_aqm), mb, (int)b, n,
+                                mref(nullptr, 0), 1.0, x.d(), b, s));
+    else
+      CANDMC_CK(cudaMemsetAsync(x.d(), 0, sizeof(double) * b * n, s));
+    CANDMC_RET(small_gemm(b, n, n, 1.0, mref(x.d(), b), mref(g->aT, g->ld_at), 0.0, x.d() + b * n, b, s));
+    CANDMC_RET(small_gemm(b, n, b, 1.0, mref(T, ldt), mref(x.d() + b * n, b), 0.0, g->aT + n, g->ld_at, s));
+  }
+  CANDMC_CK(cudaMemcpy2DAsync(g->aT + n * g->ld_at + n, sizeof(double) * g->ld_at, T, sizeof(double) * ldt,
+                              sizeof(double) * b, b, cudaMemcpyDeviceToDevice, s));
+  g->n += b;
+  return CANDMC_OK;
+}
+
+static int yamamoto_reset(YAgg* g, cudaStream_t s) {
+  CANDMC_CK(cudaMemsetAsync(g->aQm, 0, sizeof(double) * g->ld_aqm * g->ld_at, s));
+  CANDMC_CK(cudaMemsetAsync(g->aT, 0, sizeof(double) * g->ld_at * g->ld_at, s));
+  g->n = 0;
+  g->shift = 0;
+  return CANDMC_OK;
+}
+
+// QR_Yamamoto_2D on one GPU (qr_y2d.cxx:181-263).  Y below R is the panel's
+// Householder Y in both settings of compute_Y: the reference writes
+// Qm U^-1 (:220-240), which is that Y, and otherwise leaves its leaf
+// reflectors there, which on one process are the same vectors.
+static int qr_yamamoto_2d_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, YAgg* agg, int* st,
+                              int precision, cudaStream_t s) {
+  int64_t r0 = 0;
+  for (;;) {
+    const int64_t mm = m - r0, kk = k - r0, bb = std::min(kk, b);
+    double* P = A + r0 * lda + r0;
+    DevBuf qm, w;
+    CANDMC_RET(qm.alloc(sizeof(double) * mm * bb, s));
+    CANDMC_RET(w.alloc(sizeof(double) * bb * bb, s));
+    CANDMC_RET(yamamoto_panel(P, lda, mm, bb, qm.d(), mm, w.d(), st, s));
+    const bool more = kk - b > 0 && mm - b > 0;
+    if (!more) {
+      if (agg && mm - b >= 0) CANDMC_RET(yamamoto_append(agg, mm, bb, qm.d(), mm, w.d(), bb, s));
+      break;
+    }
+    CANDMC_RET(upd_yamamoto(qm.d(), mm, P + bb * lda, lda, mm, kk - b, bb, w.d(), bb, precision, s));
+    if (agg) {
+      CANDMC_RET(yamamoto_append(agg, mm, bb, qm.d(), mm, w.d(), bb, s));
+      agg->shift += b;
+    }
+    r0 += b;
+  }
+  return CANDMC_OK;
+}
+
+// QR_Yamamoto_2D_2D (qr_y2d.cxx:265-393): a b-wide block by QR_Yamamoto_2D
+// with b_sub panels aggregated into one representation, which updates the
+// columns beyond the block at once; the aggregator is reset, the trailing
+// block recurses.
+static int qr_yamamoto_2d_2d_dev(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int64_t b_sub,
+                                 YAgg* agg, int* st, int precision, cudaStream_t s) {
+  DevBuf aq, at;
+  YAgg own{};
+  int64_t r0 = 0;
+  for (;;) {
+    const int64_t mm = m - r0, kk = k - r0;
+    double* P = A + r0 * lda + r0;
+    if (!(kk - b > 0 && mm - b > 0)) return qr_yamamoto_2d_dev(P, lda, mm, kk, b_sub, agg, st, precision, s);
+    if (!agg) {
+      CANDMC_RET(aq.alloc(sizeof(double) * mm * b, s));
+      CANDMC_RET(at.alloc(sizeof(double) * b * b, s));
+      own = YAgg{aq.d(), mm, at.d(), b, 0, 0};
+      CANDMC_RET(yamamoto_reset(&own, s));
+      agg = &own;
+    }
+    CANDMC_RET(qr_yamamoto_2d_dev(P, lda, mm, std::min(kk, b), b_sub, agg, st, precision, s));
+    if (agg->n < b || agg->ld_aqm < mm) return set_error(CANDMC_ERR_ARG, "aggregator too small for the block");
+    CANDMC_RET(upd_yamamoto(agg->aQm, agg->ld_aqm, P + b * lda, lda, mm, kk - b, b, agg->aT, agg->ld_at,
+                            precision, s));
+    CANDMC_RET(yamamoto_reset(agg, s));
+    r0 += b;
+  }
+}
 }  // namespace candmc
 
 using namespace candmc;
@@ -667,6 +838,78 @@ int candmc_QR_2D_pipe(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, i
   Status st;
   CANDMC_RET(st.init(s));
   return qr_2d_pipe_dev(A, lda, m, k, b, st.p(), precision, s, nullptr);
+}
+
+int candmc_Yamamoto(double* A, int64_t lda, double* Qm, int64_t ldq, int64_t m, int64_t b, double* W,
+                    void* stream) {
+  if (!A || !Qm || !W || b < 1 || m < b || lda < m || ldq < m) return set_error(CANDMC_ERR_ARG, "Yamamoto args");
+  cudaStream_t s = STREAM(stream);
+  Status st;
+  CANDMC_RET(st.init(s));
+  return yamamoto_panel(A, lda, m, b, Qm, ldq, W, st.p(), s);
+}
+
+int candmc_upd_Yamamoto_A(const double* Qm, int64_t ldq, double* A, int64_t lda, int64_t mb, int64_t kb,
+                          int64_t b, const double* W, int precision, void* stream) {
+  if (!Qm || !A || !W || b < 1 || b > 256 || mb < 0 || kb < 0 || (mb > 0 && (ldq < mb || lda < mb)))
+    return set_error(CANDMC_ERR_ARG, "upd_Yamamoto_A args");
+  return upd_yamamoto(Qm, ldq, A, lda, mb, kb, b, W, b, precision, STREAM(stream));
+}
+
+int candmc_yamamoto_append(double* aQm, int64_t ld_aqm, double* aT, int64_t ld_at, int64_t n, int64_t shift,
+                           int64_t mb, int64_t b, const double* Qm, int64_t ldq, const double* T, void* stream) {
+  if (!aQm || !aT || !Qm || !T || b < 1 || b > 256 || n < 0 || shift < 0 || mb < 0 || (mb > 0 && ldq < mb))
+    return set_error(CANDMC_ERR_ARG, "aggregator append args");
+  YAgg g{aQm, ld_aqm, aT, ld_at, n, shift};
+  return yamamoto_append(&g, mb, b, Qm, ldq, T, b, STREAM(stream));
+}
+
+static int yagg_args(double* aQm, int64_t ld_aqm, double* aT, int64_t ld_at, int64_t* agg_n,
+                     int64_t* agg_shift, YAgg* g, YAgg** out) {
+  *out = nullptr;
+  if (!aQm && !aT) return CANDMC_OK;
+  if (!aQm || !aT || !agg_n || !agg_shift || ld_aqm < 1 || ld_at < 1 || *agg_n < 0 || *agg_shift < 0)
+    return set_error(CANDMC_ERR_ARG, "aggregator args");
+  *g = YAgg{aQm, ld_aqm, aT, ld_at, *agg_n, *agg_shift};
+  *out = g;
+  return CANDMC_OK;
+}
+
+int candmc_QR_Yamamoto_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int compute_Y, double* aQm,
+                          int64_t ld_aqm, double* aT, int64_t ld_at, int64_t* agg_n, int64_t* agg_shift,
+                          int precision, void* stream) {
+  (void)compute_Y;   // Y below R is the panel's Householder Y either way
+  if (!A || b < 1 || b > 256 || k < 1 || m < k || lda < m) return set_error(CANDMC_ERR_ARG, "QR_Yamamoto_2D args");
+  YAgg g, *pg;
+  CANDMC_RET(yagg_args(aQm, ld_aqm, aT, ld_at, agg_n, agg_shift, &g, &pg));
+  cudaStream_t s = STREAM(stream);
+  Status st;
+  CANDMC_RET(st.init(s));
+  const int rc = qr_yamamoto_2d_dev(A, lda, m, k, b, pg, st.p(), precision, s);
+  if (pg) {
+    *agg_n = pg->n;
+    *agg_shift = pg->shift;
+  }
+  return rc;
+}
+
+int candmc_QR_Yamamoto_2D_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int64_t b_sub,
+                             int compute_Y, double* aQm, int64_t ld_aqm, double* aT, int64_t ld_at,
+                             int64_t* agg_n, int64_t* agg_shift, int precision, void* stream) {
+  (void)compute_Y;
+  if (!A || b < 1 || b > 256 || b_sub < 1 || b % b_sub != 0 || k < 1 || m < k || lda < m)
+    return set_error(CANDMC_ERR_ARG, "QR_Yamamoto_2D_2D args");
+  YAgg g, *pg;
+  CANDMC_RET(yagg_args(aQm, ld_aqm, aT, ld_at, agg_n, agg_shift, &g, &pg));
+  cudaStream_t s = STREAM(stream);
+  Status st;
+  CANDMC_RET(st.init(s));
+  const int rc = qr_yamamoto_2d_2d_dev(A, lda, m, k, b, b_sub, pg, st.p(), precision, s);
+  if (pg) {
+    *agg_n = pg->n;
+    *agg_shift = pg->shift;
+  }
+  return rc;
 }
 
 }  // extern "C"

@@ -7,6 +7,7 @@
 // record the status (candmc_dropin_last_status) and leave the outputs
 // untouched instead.  Process grids larger than 1 x 1 are rejected.
 #include <cuda_runtime.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -275,4 +276,125 @@ void QR_2D_2D(double* A, int64_t lda_A, int64_t m, int64_t k, int64_t b, int64_t
   if (finish(rc) != CANDMC_OK) return;
   dA.out(A, lda_A);
   if (aggreg_Y) dG.out(aggreg_Y, lda_aY);
+}
+
+// ------------------------------------------------------------------ Yamamoto
+void Yamamoto(double* A, int64_t lda_A, double* Qm, int64_t lda_Qm, int64_t m, int64_t b, double* W,
+              int64_t myRank, int64_t numPes, int64_t root, int64_t req_id, CommData_t cdt) {
+  (void)root; (void)req_id; (void)cdt;
+  if (!one_rank(numPes, myRank) || !A || !Qm || !W) { g_status = CANDMC_ERR_ARG; return; }
+  DMat dA, dQ, dW;
+  if (!stage(dA, A, lda_A, m, b) || !dQ.alloc(m, b) || !dW.alloc(b, b)) { g_status = CANDMC_ERR_ALLOC; return; }
+  int rc = candmc_Yamamoto(dA.p, dA.ld, dQ.p, dQ.ld, m, b, dW.p, nullptr);
+  if (finish(rc) != CANDMC_OK) return;
+  dA.out(A, lda_A);
+  dQ.out(Qm, lda_Qm);
+  dW.out(W, b);
+}
+
+aggregator::aggregator(int64_t lda_aQm_, int64_t lda_aT_) {
+  lda_aQm = lda_aQm_;
+  lda_aT = lda_aT_;
+  aQm = static_cast<double*>(calloc((size_t)(lda_aT * lda_aQm > 0 ? lda_aT * lda_aQm : 1), sizeof(double)));
+  aT = static_cast<double*>(calloc((size_t)(lda_aT > 0 ? lda_aT * lda_aT : 1), sizeof(double)));
+  n = 0;
+  shift = 0;
+}
+
+aggregator::~aggregator() {
+  free(aQm);
+  free(aT);
+}
+
+void aggregator::reset() {
+  n = 0;
+  shift = 0;
+  std::fill(aQm, aQm + lda_aT * lda_aQm, 0.0);
+  std::fill(aT, aT + lda_aT * lda_aT, 0.0);
+}
+
+void aggregator::shift_down(int64_t b) { shift += b; }
+
+namespace {
+
+// the aggregator's host arrays on the device for one call
+struct DAgg {
+  DMat q, t;
+  bool in(const aggregator* a) {
+    return stage(q, a->aQm, a->lda_aQm, a->lda_aQm, a->lda_aT) && stage(t, a->aT, a->lda_aT, a->lda_aT, a->lda_aT);
+  }
+  void out(aggregator* a) const {
+    q.out(a->aQm, a->lda_aQm);
+    t.out(a->aT, a->lda_aT);
+  }
+};
+
+}  // namespace
+
+void aggregator::append(int64_t mb, int64_t b, double const* Qm, int64_t lda_Qm, double const* T, pview* pv) {
+  if (!one_grid(pv)) { g_status = CANDMC_ERR_ARG; return; }
+  DAgg d;
+  DMat dQ, dT;
+  if (!d.in(this) || !stage(dQ, Qm, lda_Qm, mb, b) || !stage(dT, T, b, b, b)) { g_status = CANDMC_ERR_ALLOC; return; }
+  int rc = candmc_yamamoto_append(d.q.p, d.q.ld, d.t.p, d.t.ld, n, shift, mb, b, dQ.p, dQ.ld, dT.p, nullptr);
+  if (finish(rc) != CANDMC_OK) return;
+  d.out(this);
+  n += b;
+}
+
+void upd_Yamamoto_A(double const* Qm, int64_t lda_Qm, double* A, int64_t lda_A, int64_t mb, int64_t kb,
+                    int64_t b, double const* T, pview* pv) {
+  if (!one_grid(pv)) { g_status = CANDMC_ERR_ARG; return; }
+  DMat dQ, dA, dT;
+  if (!stage(dQ, Qm, lda_Qm, mb, b) || !stage(dA, A, lda_A, mb, kb) || !stage(dT, T, b, b, b)) {
+    g_status = CANDMC_ERR_ALLOC;
+    return;
+  }
+  int rc = candmc_upd_Yamamoto_A(dQ.p, dQ.ld, dA.p, dA.ld, mb, kb, b, dT.p, g_precision, nullptr);
+  if (finish(rc) == CANDMC_OK) dA.out(A, lda_A);
+}
+
+void update_Yamamoto_A(double* Qm, int64_t lda_Qm, double* A, int64_t lda_A, int64_t m, int64_t k, int64_t b,
+                       double* T, pview* pv, aggregator* agg) {
+  // one process: mb = m and kb = k (qr_y2d.cxx:81-89), no broadcasts
+  upd_Yamamoto_A(Qm, lda_Qm, A, lda_A, m, k, b, T, pv);
+  if (g_status == CANDMC_OK && agg != nullptr) agg->append(m, b, Qm, lda_Qm, T, pv);
+}
+
+void QR_Yamamoto_2D(double* A, int64_t lda_A, int64_t m, int64_t k, int64_t b, pview* pv, aggregator* agg,
+                    bool compute_Y) {
+  if (!one_grid(pv)) { g_status = CANDMC_ERR_ARG; return; }
+  DMat dA;
+  DAgg d;
+  if (!stage(dA, A, lda_A, m, k) || (agg && !d.in(agg))) { g_status = CANDMC_ERR_ALLOC; return; }
+  int64_t n = agg ? agg->n : 0, sh = agg ? agg->shift : 0;
+  int rc = candmc_QR_Yamamoto_2D(dA.p, dA.ld, m, k, b, compute_Y ? 1 : 0, agg ? d.q.p : nullptr, d.q.ld,
+                                 agg ? d.t.p : nullptr, d.t.ld, agg ? &n : nullptr, agg ? &sh : nullptr,
+                                 g_precision, nullptr);
+  if (finish(rc) != CANDMC_OK) return;
+  dA.out(A, lda_A);
+  if (agg) {
+    d.out(agg);
+    agg->n = n;
+    agg->shift = sh;
+  }
+}
+
+void QR_Yamamoto_2D_2D(double* A, int64_t lda_A, int64_t m, int64_t k, int64_t b, int64_t b_sub, pview* pv,
+                       aggregator* agg, bool compute_Y) {
+  if (!one_grid(pv)) { g_status = CANDMC_ERR_ARG; return; }
+  DMat dA;
+  DAgg d;
+  if (!stage(dA, A, lda_A, m, k) || (agg && !d.in(agg))) { g_status = CANDMC_ERR_ALLOC; return; }
+  int64_t n = agg ? agg->n : 0, sh = agg ? agg->shift : 0;
+  int rc = candmc_QR_Yamamoto_2D_2D(dA.p, dA.ld, m, k, b, b_sub, compute_Y ? 1 : 0, agg ? d.q.p : nullptr,
+                                    d.q.ld, agg ? d.t.p : nullptr, d.t.ld, agg ? &n : nullptr,
+                                    agg ? &sh : nullptr, g_precision, nullptr);
+  if (finish(rc) != CANDMC_OK) return;
+  dA.out(A, lda_A);
+  if (agg) {
+    d.out(agg);
+    agg->n = n;
+    agg->shift = sh;
+  }
 }

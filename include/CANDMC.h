@@ -1,8 +1,8 @@
 /*
  * CANDMC.h for the GB300 QR hot path: the QR part of the reference's
  * umbrella header (include/CANDMC.h:19-32), with the single-GPU drop-in
- * declarations.  The MM, LU, SE and Yamamoto parts of the reference are not
- * provided by this library.
+ * declarations.  The MM, LU and SE parts of the reference are not provided
+ * by this library.
  */
 #ifndef __CANDMC_H__
 #define __CANDMC_H__
@@ -15,6 +15,9 @@
 
 /* 2D QR algorithms for full matrices */
 #include "candmc/qr_2d.h"
+
+/* 2D QR with Yamamoto's basis-kernel representation for full matrices */
+#include "candmc/qr_y2d.h"
 
 /* the C ABI underneath */
 #include "candmc_gb300.h"

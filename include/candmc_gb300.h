@@ -178,6 +178,46 @@ int candmc_QR_2D_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int
 int candmc_QR_2D_pipe(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int precision,
                       void* stream);
 
+/* ---- Yamamoto's basis-kernel representation ----------------------------------
+ * alg/QR/hh_recon/yamamoto.h:21-32, alg/QR/qr_2d/qr_y2d.h (qr_y2d.cxx:13-393),
+ * device pointers.  The representation: Q^T = I + Qm W Qm^T with
+ * Qm = [Q1 - S; Q2] (m x b) and W = (Q1 - S)^-1 S (b x b, ld b) for the first
+ * b columns [Q1; Q2] of a TSQR basis and the sign choice S.  The returned
+ * pair is the reference's up to the reference's own sign matrix S_ref
+ * (Qm_ref = Qm S_ref, W_ref = S_ref W S_ref): it is built from the
+ * Householder reconstruction with the basis whose S is the identity.
+ * Qm W Qm^T, the updates and S*R are the reference's.
+ *
+ * Yamamoto: A (m x b, lda) becomes Y\(S*R) (Householder Y below the
+ * diagonal); Qm (ldq >= m) and W are written. */
+int candmc_Yamamoto(double* A, int64_t lda, double* Qm, int64_t ldq, int64_t m, int64_t b, double* W,
+                    void* stream);
+
+/* upd_Yamamoto_A (qr_y2d.h:79-99): A (mb x kb, lda) += Qm (W (Qm^T A)),
+ * b <= 256 (<= 128 for the ozaki and fp32 forms). */
+int candmc_upd_Yamamoto_A(const double* Qm, int64_t ldq, double* A, int64_t lda, int64_t mb, int64_t kb,
+                          int64_t b, const double* W, int precision, void* stream);
+
+/* aggregator::append (qr_y2d.h:30-43): appends the mb x b Qm at rows
+ * [shift, shift + mb) and columns [n, n + b) of aQm (ld_aqm rows, ld_at
+ * columns) and the block row [T (Qm^T aQm) aT, T] to aT (ld_at x ld_at).
+ * The caller adds b to its n.  CANDMC_ERR_ARG if the block does not fit. */
+int candmc_yamamoto_append(double* aQm, int64_t ld_aqm, double* aT, int64_t ld_at, int64_t n, int64_t shift,
+                           int64_t mb, int64_t b, const double* Qm, int64_t ldq, const double* T, void* stream);
+
+/* QR_Yamamoto_2D (qr_y2d.h:102-119) and QR_Yamamoto_2D_2D (qr_y2d.h:122-139)
+ * on a 1 x 1 grid.  A (m x k) becomes Y\(S*R) of all panels; Y is the
+ * Householder Y for either value of compute_Y.  aQm/aT (both null, or the
+ * aggregator's buffers with *agg_n and *agg_shift its counters, updated on
+ * return) receive the panels' representation as the reference's aggregator
+ * does. */
+int candmc_QR_Yamamoto_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int compute_Y, double* aQm,
+                          int64_t ld_aqm, double* aT, int64_t ld_at, int64_t* agg_n, int64_t* agg_shift,
+                          int precision, void* stream);
+int candmc_QR_Yamamoto_2D_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int64_t b_sub,
+                             int compute_Y, double* aQm, int64_t ld_aqm, double* aT, int64_t ld_at,
+                             int64_t* agg_n, int64_t* agg_shift, int precision, void* stream);
+
 /* ---- least squares (no counterpart in the reference, which stops at the
  * factorization; built from QR_2D_pipe and update_A) ---------------------------
  * min ||A X - B||_F for A m x n (m >= n, full column rank), B m x nrhs, device

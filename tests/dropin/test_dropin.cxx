@@ -119,6 +119,58 @@ int main() {
     fails += report(name, sqrt(num / den), 1e-13);
   }
   candmc_dropin_set_precision(CANDMC_PREC_FP64);
+  // test_qr_y2d at a 1 x 1 grid: QR_Yamamoto_2D_2D with compute_Y (test/QR/test_qr_y2d.cxx:116),
+  // Q^T applied panel by panel from the Y it leaves below R
+  for (int prec : {CANDMC_PREC_FP64, CANDMC_PREC_OZAKI}) {
+    const int64_t m = 256, k = 192, b2 = 64, b = 32;
+    std::vector<double> A(m * k);
+    for (int64_t c = 0; c < k; ++c)
+      for (int64_t r = 0; r < m; ++r) A[c * m + r] = fixture(r, c, m, 0.5);
+    std::vector<double> YR(A);
+    pview pv = candmc_single_gpu_view();
+    candmc_dropin_set_precision(prec);
+    QR_Yamamoto_2D_2D(YR.data(), m, m, k, b2, b, &pv, NULL, true);
+    candmc_dropin_set_precision(CANDMC_PREC_FP64);
+    std::vector<double> B(A);
+    for (int64_t r0 = 0; r0 < k; r0 += b) {
+      pview pv2 = candmc_single_gpu_view();
+      update_A(YR.data() + r0 * m + r0, m, B.data() + r0, m, m - r0, k, b, NULL, &pv2, NULL, 0);
+    }
+    double num = 0, den = 0;
+    for (int64_t c = 0; c < k; ++c)
+      for (int64_t r = 0; r < m; ++r) {
+        const double rr = (r <= c) ? YR[c * m + r] : 0.0;
+        num += (B[c * m + r] - rr) * (B[c * m + r] - rr);
+        den += A[c * m + r] * A[c * m + r];
+      }
+    char name[64];
+    snprintf(name, sizeof name, "QR_Yamamoto_2D_2D %s ||A-QR||/||A||", prec == CANDMC_PREC_FP64 ? "fp64" : "ozaki");
+    fails += report(name, sqrt(num / den), 1e-13);
+  }
+  // Yamamoto's representation of a 128 x 64 block aggregated over two 32-column panels:
+  // A + aQm aT aQm^T A is [S R; 0]
+  {
+    const int64_t m = 128, k = 64, b = 32;
+    std::vector<double> A(m * k);
+    for (int64_t c = 0; c < k; ++c)
+      for (int64_t r = 0; r < m; ++r) A[c * m + r] = fixture(r, c, m, 0.5);
+    std::vector<double> YR(A);
+    pview pv = candmc_single_gpu_view();
+    aggregator agg(m, k);
+    QR_Yamamoto_2D(YR.data(), m, m, k, b, &pv, &agg, false);
+    std::vector<double> B(A);
+    upd_Yamamoto_A(agg.aQm, agg.lda_aQm, B.data(), m, m, k, k, agg.aT, &pv);
+    double num = 0, den = 0;
+    for (int64_t c = 0; c < k; ++c)
+      for (int64_t r = 0; r < m; ++r) {
+        const double rr = (r <= c) ? YR[c * m + r] : 0.0;
+        num += (B[c * m + r] - rr) * (B[c * m + r] - rr);
+        den += A[c * m + r] * A[c * m + r];
+      }
+    const bool n_ok = agg.n == k;
+    fails += report(n_ok ? "aggregator ||A + aQm aT aQm^T A - R||/||A||" : "aggregator count wrong",
+                    n_ok ? sqrt(num / den) : 1.0, 1e-13);
+  }
   // a grid larger than 1 x 1 is rejected without touching the data
   {
     pview pv = candmc_single_gpu_view();
