@@ -49,3 +49,27 @@ def test_argument_errors_without_gpu(built):
     assert lib.candmc_hh_recon_qr(None, 10, 10, 4, None, None, None) == 1
     assert lib.candmc_QR_2D(None, 10, 10, 10, 4, None, 0, 0, None) == 1
     assert lib.candmc_hh_recon_qr_host(None, 10, 5, 8, None, None) == 1
+
+
+def test_yamamoto_argument_errors_without_gpu(built):
+    """The Yamamoto entry points validate their arguments, including the
+    aggregator's buffers and counters, before any device call."""
+    import ctypes
+    from candmc_gb300 import _abi
+    lib = _abi.load()
+    dummy = ctypes.c_void_p(16)   # never dereferenced: every call below fails validation first
+    n, sh = ctypes.c_int64(0), ctypes.c_int64(0)
+    # Yamamoto: null pointers, ldq < m
+    assert lib.candmc_Yamamoto(None, 10, dummy, 10, 10, 4, dummy, None) == 1
+    assert lib.candmc_Yamamoto(dummy, 10, dummy, 5, 10, 4, dummy, None) == 1
+    # upd_Yamamoto_A: b above 256
+    assert lib.candmc_upd_Yamamoto_A(dummy, 300, dummy, 300, 300, 10, 257, dummy, 0, None) == 1
+    # aggregator append: negative counters
+    assert lib.candmc_yamamoto_append(dummy, 10, dummy, 4, -1, 0, 10, 4, dummy, 10, dummy, None) == 1
+    # QR_Yamamoto_2D: aQm without aT, and counters missing
+    assert lib.candmc_QR_Yamamoto_2D(dummy, 10, 10, 8, 4, 0, dummy, 10, None, 8, ctypes.byref(n),
+                                     ctypes.byref(sh), 0, None) == 1
+    assert lib.candmc_QR_Yamamoto_2D(dummy, 10, 10, 8, 4, 0, dummy, 10, dummy, 8, None, None, 0, None) == 1
+    # QR_Yamamoto_2D_2D: b not a multiple of b_sub, m < k
+    assert lib.candmc_QR_Yamamoto_2D_2D(dummy, 10, 10, 8, 6, 4, 0, None, 0, None, 0, None, None, 0, None) == 1
+    assert lib.candmc_QR_Yamamoto_2D_2D(dummy, 10, 6, 8, 4, 4, 0, None, 0, None, 0, None, None, 0, None) == 1
