@@ -14,21 +14,23 @@
 //
 // The trailing matrix is held as float pairs (hi, lo) ("df64", ~48 bits)
 // during the emulated factorization, so no epilogue needs the GB300's slow
-// FP64 pipe: groups are combined, scaled and subtracted with FP32 TwoSum
-// arithmetic.  Finished rows (the panel's R block) are written back as FP64.
+// FP64 pipe: the five accumulators are combined exactly (integer/fraction
+// split, fast TwoSum), scaled by a power of two and accumulated or subtracted
+// in df64.  Finished rows (the panel's R block) are written back as FP64.
 //
 // Kernel layout (k_oz_mma): persistent CTAs (at most one per SM) over work
-// items of one 128 x 96 output tile and K range each; 10 warps.  Operand
+// items of one 128 x 96 output tile and K range each; 14 warps.  Operand
 // slices are pre-sliced in global memory in the UMMA "K-major, no swizzle"
 // core-matrix order, so each K16 step of a tile is a contiguous 4 KB (A, 128
 // rows) and 3 KB (B, 96 rows) block per slice: a producer warp streams them
 // with bulk asynchronous copies into a 4-stage shared-memory ring, an MMA
 // warp issues the 28 tcgen05.mma of a step and commits them to the stage's
 // "empty" mbarrier (and, at the end of an exact-accumulation group, to the
-// epilogue's "full" mbarrier), and eight epilogue warps drain TMEM, release it
-// and combine in df64 while the next group's MMAs run.  Every wait is
-// bounded; a wait that runs out sets the status word, the roles stop, the
-// MMA warp waits for its last MMAs, and the CTA frees its TMEM and returns.
+// epilogue's "full" mbarrier), and twelve epilogue warps drain and combine
+// the accumulators and release them; the df64 read-modify-write of C (MODE
+// 1) then overlaps the next group's MMAs.  Every wait is bounded; a wait that
+// runs out sets the status word, the roles stop, the MMA warp waits for its
+// last MMAs, and the CTA frees its TMEM and returns.
 #include <cuda_bf16.h>
 #include <math.h>
 

@@ -12,14 +12,18 @@
 //  * leaves of at most leaf_rows rows, one CTA each: b Householder steps in
 //    the column-owner schedule below, which also yields the leaf's
 //    compact-WY T (T^-1 from the Gram matrix V^T V);
-//  * a fan-in-4 tree (last arriver combines, no waiting): the node stacks up
-//    to four R factors and runs b Householder steps on the stacked matrix (the
-//    zeros below the children's diagonals stay zero); with V = [I; V_2..V_4]
-//    the node's Q blocks are Q_1 = I - T and Q_k = -V_k T (all upper
-//    triangular), so no explicit-Q pass is needed;
-//  * the CTA that completes the root forms Q1_top = C0 - V0 (T0 (V0^T C0)),
-//    C0 the chain of Q_1 blocks, runs the sign-choice LU and writes L\(S R),
-//    T, W and U^-1;
+//  * a fan-in-4 tree: the node stacks up to four R factors and runs b
+//    Householder steps on the stacked matrix (the zeros below the children's
+//    diagonals stay zero); with V = [I; V_2..V_4] the node's Q blocks are
+//    Q_1 = I - T and Q_k = -V_k T (all upper triangular), so no explicit-Q
+//    pass is needed.  Two schedules: k_hr6_pipe, where every node is a CTA
+//    that starts column j as soon as its children have published it (the
+//    levels overlap; roles by atomic ticket, bounded waits), and
+//    k_hr4_leaf_tree, where the last CTA to arrive combines a node;
+//  * the root: Q1_top = (I - V0 T0 V0^T) Q_1^(1) ... Q_1^(depth) on the top
+//    b rows, then the sign-choice LU of Q1_top - S, and L\(S R), T, W and
+//    U^-1.  In k_hr6_pipe leaf 0 and the nodes on its path build Q1_top as a
+//    prefix product while they finish, and one extra CTA solves the root;
 //  * kernel 2: each leaf multiplies its root-to-leaf chain of Q blocks into
 //    U^-1 (M) and writes Y = [M; 0] - V (T (V_top^T M)).
 // The Householder factor is canonical, so the result equals the binary-tree
