@@ -20,7 +20,16 @@
 // The first call on a device does a one-time set-up with that device
 // current: it looks up the device address of the array and raises the leaf
 // kernel's shared-memory limit.  Make that first call before any stream
-// capture begins.
+// capture begins.  The set-up is guarded by a mutex, so first calls from
+// several host threads are safe (the GPU work itself must still not overlap).
+//
+// The kernels record a numeric failure (a non-finite U^-1 in the sign-choice
+// LU) in a status word inside the shared scratch.  This entry point does not
+// read that word back, since that would synchronise the caller's stream; the
+// next call clears it.  A caller that needs the check tests W and T for
+// non-finite values.
+#include <mutex>
+
 #include "kernels.cuh"
 
 namespace candmc {
@@ -52,11 +61,13 @@ struct DeviceScratch {
   double* base = nullptr;
 };
 static DeviceScratch g_dev[64];
+static std::mutex g_dev_mutex;
 
 int setup_device(double** base) {
   int dev = 0;
   CANDMC_CK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return set_error(CANDMC_ERR_ARG, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_dev_mutex);
   if (!g_dev[dev].ready) {
     void* p = nullptr;
     CANDMC_CK(cudaGetSymbolAddress(&p, g_hr_scratch));

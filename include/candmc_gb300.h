@@ -88,8 +88,11 @@ int candmc_hh_recon_qr_host(double* A, int64_t lda, int64_t m, int64_t b, double
  * GPU that loads the library until exit.  Limits: 1 <= b <= 32 and
  * b <= m <= 8192; larger sizes return CANDMC_ERR_ARG.  All calls share that
  * array, so calls that overlap on the GPU race: serialize them.  The first
- * call on a device sets up that device (looks up the array's address); make
- * it before any stream capture begins. */
+ * call on a device sets up that device (looks up the array's address, under
+ * a mutex); make it before any stream capture begins.  A numeric failure in
+ * the kernels (non-finite U^-1) is not reported by the return code: the call
+ * does not read its device status back, so check W and T for non-finite
+ * values where that matters. */
 int candmc_hh_recon_qr_noalloc(double* A, int64_t lda, int64_t m, int64_t b, double* W, double* T,
                                void* stream);
 

@@ -143,6 +143,15 @@ def construct_Q1(blocks_Y, taus, tree, b, k, root=0):
     return out
 
 
+def apply_tsqr_QT(YR, tau, B, b):
+    """B <- Q^T B for the single-rank TSQR factor (apply_tsqr_QT.cxx:74-82:
+    dormqr('L','T') with the leaf's reflectors): B - Y T^T (Y^T B), T from
+    dlarft.  YR holds the dgeqrf-form reflectors below its diagonal."""
+    Y = lp.unit_lower(YR, b)
+    T = lp.dlarft(Y, tau)
+    return B - Y @ (T.T @ (Y.T @ B))
+
+
 # --------------------------------------------------------------------------
 # Householder reconstruction (alg/QR/hh_recon/hh_recon.cxx)
 # --------------------------------------------------------------------------

@@ -155,7 +155,7 @@ def dtpqrt_tri(R1, R2):
     Restates the unblocked dtpqrt2 with a triangular ("pentagonal", l = n)
     bottom block: reflector j is [e_j; V[0:j+1, j]].  R1 becomes R, R2 becomes
     V (upper triangular).  Returns tau (n,).  dtpqrt stores the same
-    reflectors plus the block-diagonal T; T is rebuilt by `dtp_larft` below.
+    reflectors plus the block-diagonal T; T is rebuilt by `dtpqrt_T` below.
     """
     n = R1.shape[1]
     tau = np.zeros(n)
@@ -169,6 +169,21 @@ def dtpqrt_tri(R1, R2):
             R1[j, j + 1:] -= t * w
             R2[:j + 1, j + 1:] -= t * np.outer(v, w)
     return tau
+
+
+def dtpqrt_T(V, tau, nb):
+    """The T output of dtpqrt (nb x n, ld nb) for the dtpqrt_tri reflectors:
+    column c holds the upper triangle of the nb-wide diagonal block of the
+    compact-WY factor of Y = [I; V] that contains c (the T of that block of
+    reflectors alone); entries below each block's diagonal are zero."""
+    n = V.shape[1]
+    Y = np.vstack([np.eye(n), np.triu(V)])
+    T = dlarft(Y, tau)
+    out = np.zeros((nb, n))
+    for c in range(n):
+        q0 = (c // nb) * nb
+        out[:c - q0 + 1, c] = T[q0:c + 1, c]
+    return out
 
 
 def dtpmqrt_left_notrans(V, tau, top, bottom):
