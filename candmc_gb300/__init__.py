@@ -142,6 +142,33 @@ def construct_Q1(Y, tau, k=None, stream=None):
     return Q1
 
 
+def tree_tsqr(A, T=None, stream=None):
+    """QR of the stacked [R1; R2] (alg/QR/tsqr/bitree_tsqr.h:16-19, dtpqrt's
+    contract): A (2b x b) gets R over R1's and V over R2's upper triangle, its
+    strictly-lower entries untouched.  Returns T (min(b,16) x b), dtpqrt's
+    block-diagonal factor."""
+    m, b = A.shape
+    if m != 2 * b:
+        raise ValueError("tree_tsqr: A must be 2b x b")
+    pa, lda = _dev(A, "A")
+    if lda != 2 * b:
+        raise ValueError("tree_tsqr: the leading dimension of A must be 2b")
+    nb = min(b, 16)
+    T = _torch().zeros((b, nb), dtype=_torch().float64, device=A.device).t() if T is None else T
+    check(lib().candmc_tree_tsqr(pa, b, _dev(T, "T")[0], _stream(stream)), "tree_tsqr")
+    return T
+
+
+def apply_tsqr_QT(Y, tau, B, stream=None):
+    """B <- Q^T B for the single-rank TSQR factor (alg/QR/tsqr/bitree_tsqr.h:126-138)."""
+    m, b = Y.shape
+    py, ldy = _dev(Y, "Y")
+    pb, ldb = _dev(B, "B")
+    check(lib().candmc_apply_tsqr_QT(py, ldy, tau.data_ptr(), pb, ldb, m, b, B.shape[1], _stream(stream)),
+          "apply_tsqr_QT")
+    return B
+
+
 def compute_invT_from_W(W, Y1, stream=None):
     """T^-T from W and Y1 (alg/QR/hh_recon/hh_recon.h:13-15): solves W^T X = -Y1."""
     b = W.shape[0]

@@ -666,6 +666,59 @@ int candmc_bitree_tsqr(double* A, int64_t lda, double* R, double* tau, int64_t m
   return CANDMC_OK;
 }
 
+// ---- tree_tsqr: QR of two stacked upper-triangular blocks ----------------
+// [R1; R2] (2b x b, ld 2b).  Only the upper triangles are read; the stage
+// kernel copies them into a dense 2b x b panel with zeros below, which the
+// Householder reconstruction factors; the store kernel writes R over R1's
+// upper triangle, the reflector block V (upper triangular) over R2's, and
+// the block-diagonal T in dtpqrt's nb x b layout, leaving every strictly-
+// lower entry of the caller's buffer as it was (bitree_tsqr.cxx:20-34).
+__global__ void k_tree_stage(const double* A, int64_t b, double* P) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 2 * b * b) return;
+  const int64_t i = idx % (2 * b), j = idx / (2 * b);
+  const int64_t r = i < b ? i : i - b;
+  P[j * 2 * b + i] = (r <= j) ? A[j * 2 * b + i] : 0.0;
+}
+
+__global__ void k_tree_store(const double* P, const double* T, int64_t b, int64_t nb, double* A,
+                             double* Tout) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < 2 * b * b) {
+    const int64_t i = idx % (2 * b), j = idx / (2 * b);
+    const int64_t r = i < b ? i : i - b;
+    if (r <= j) A[j * 2 * b + i] = P[j * 2 * b + i];
+  }
+  if (Tout && idx < nb * b) {
+    const int64_t r = idx % nb, c = idx / nb, q0 = (c / nb) * nb;
+    if (q0 + r <= c) Tout[c * nb + r] = T[c * b + q0 + r];
+  }
+}
+
+int candmc_tree_tsqr(double* A, int64_t b, double* T, void* stream) {
+  if (!A || b < 1) return set_error(CANDMC_ERR_ARG, "tree_tsqr args");
+  cudaStream_t s = STREAM(stream);
+  const int64_t nb = std::min<int64_t>(b, 16);
+  Status st;
+  CANDMC_RET(st.init(s));
+  DevBuf P, Tf;
+  CANDMC_RET(P.alloc(sizeof(double) * 2 * b * b, s));
+  CANDMC_RET(Tf.alloc(sizeof(double) * b * b, s));
+  const unsigned grid = (unsigned)((2 * b * b + 255) / 256);
+  {
+    ProfScope ps(CANDMC_KCLASS_SMALL, 16.0 * b * b, s);
+    k_tree_stage<<<grid, 256, 0, s>>>(A, b, P.d());
+  }
+  CANDMC_CK(cudaGetLastError());
+  CANDMC_RET(hh_recon_dev(P.d(), 2 * b, 2 * b, b, nullptr, 0, Tf.d(), b, st.p(), CANDMC_PREC_FP64, s));
+  {
+    ProfScope ps(CANDMC_KCLASS_SMALL, 16.0 * b * b, s);
+    k_tree_store<<<grid, 256, 0, s>>>(P.d(), Tf.d(), b, nb, A, T);
+  }
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
 int candmc_construct_Q1(const double* Y, int64_t ldy, const double* tau, double* Q1, int64_t ldq,
                         int64_t m, int64_t b, int64_t k, void* stream) {
   if (!Y || !tau || !Q1 || b < 1 || k < 1 || k > b || m < b || ldy < m || ldq < m)

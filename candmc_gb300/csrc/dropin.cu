@@ -93,24 +93,20 @@ void local_tsqr(double* A, double* R, int64_t const m, int64_t const b, int64_t 
 }
 
 void tree_tsqr(double* A, double* buf, int64_t const b, double* tau) {
-  (void)buf;
-  // QR of the stacked [R1; R2] (2b x b, ld 2b): R over V, and the block-diagonal
-  // T of dtpqrt (b x min(b, TAU_BLK) blocks, ld min(b, TAU_BLK)).
+  (void)buf;   // the reference's dtpqrt workspace
+  // QR of the stacked [R1; R2] (2b x b, ld 2b) with dtpqrt's contract: the
+  // upper triangles are read and overwritten (R over V), the strictly-lower
+  // entries are left alone, and tau receives the block-diagonal T.
   const int64_t m = 2 * b, nbk = std::min<int64_t>(b, TAU_BLK);
-  DMat dA, dW, dT;
-  if (!stage(dA, A, m, m, b) || !dW.alloc(b, b) || !dT.alloc(b, b)) { g_status = CANDMC_ERR_ALLOC; return; }
-  int rc = candmc_hh_recon_qr(dA.p, dA.ld, m, b, dW.p, dT.p, nullptr);
+  DMat dA, dT;
+  if (!stage(dA, A, m, m, b) || (tau && !stage(dT, tau, nbk, nbk, b))) {
+    g_status = CANDMC_ERR_ALLOC;
+    return;
+  }
+  int rc = candmc_tree_tsqr(dA.p, b, tau ? dT.p : nullptr, nullptr);
   if (finish(rc) != CANDMC_OK) return;
   dA.out(A, m);
-  if (tau) {
-    std::vector<double> T((size_t)b * b);
-    dT.out(T.data(), b);
-    for (int64_t c = 0; c < b; ++c) {
-      const int64_t q0 = (c / nbk) * nbk;
-      for (int64_t r = 0; r < nbk; ++r)
-        tau[c * nbk + r] = (q0 + r <= c) ? T[c * b + q0 + r] : 0.0;
-    }
-  }
+  if (tau) dT.out(tau, nbk);
 }
 
 void construct_Q1(double const* Y, int64_t const lda_Y, double const* tau, double* Q1,

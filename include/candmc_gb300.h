@@ -106,6 +106,17 @@ int candmc_hh_recon_qr_noalloc(double* A, int64_t lda, int64_t m, int64_t b, dou
 int candmc_bitree_tsqr(double* A, int64_t lda, double* R, double* tau, int64_t m, int64_t b,
                        int output_Y, void* stream);
 
+/* tree_tsqr: alg/QR/tsqr/bitree_tsqr.h:16-19 (bitree_tsqr.cxx:20-34, LAPACK
+ * dtpqrt(b, b, b, min(b,16)) on the stacked [R1; R2]).  A (2b x b, ld 2b, device)
+ * holds R1 over R2; only their upper triangles are read.  On return R1's upper
+ * triangle holds R, R2's upper triangle holds the reflector block V (the
+ * reflectors are [e_j; V(:,j)]), and every strictly-lower entry of A is as it
+ * was.  T (nullable; min(b,16) x b, ld min(b,16)) receives dtpqrt's
+ * block-diagonal factor: for each min(b,16)-wide group of columns, the upper
+ * triangle of that group's compact-WY T; entries below it are not written.
+ * The reference's buf workspace argument is not needed. */
+int candmc_tree_tsqr(double* A, int64_t b, double* T, void* stream);
+
 /* construct_Q1 at numPes == 1: alg/QR/tsqr/bitree_tsqr.h:91-104
  * (construct_tsqr_Q.cxx:87-108, dorgqr): Q1 (m x k, ld ldq) = first k columns
  * of Q = H_0...H_{b-1} from the reflectors in Y (lower part of a Y\R buffer)
