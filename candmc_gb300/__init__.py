@@ -169,6 +169,18 @@ def apply_tsqr_QT(Y, tau, B, stream=None):
     return B
 
 
+def tau_recon(structure, Y, nrow=None, stream=None):
+    """tau of the Householder vectors in Y (alg/shared/util.h:675-680):
+    structure 'R', 'L' (below the diagonal) or 'U' (rows 0..i)."""
+    rows, ncol = Y.shape
+    nrow = rows if nrow is None else nrow
+    tau = _torch().empty(ncol, dtype=_torch().float64, device=Y.device)
+    py, ldy = _dev(Y, "Y")
+    check(lib().candmc_tau_recon(structure.encode() if isinstance(structure, str) else structure, ncol, nrow,
+                                 ldy, py, tau.data_ptr(), _stream(stream)), "tau_recon")
+    return tau
+
+
 def compute_invT_from_W(W, Y1, stream=None):
     """T^-T from W and Y1 (alg/QR/hh_recon/hh_recon.h:13-15): solves W^T X = -Y1."""
     b = W.shape[0]

@@ -25,6 +25,7 @@ SIGNATURES = {
     "candmc_hh_recon_qr_noalloc": [_vp, _i64, _i64, _i64, _vp, _vp, _vp],
     "candmc_bitree_tsqr": [_vp, _i64, _vp, _vp, _i64, _i64, _int, _vp],
     "candmc_tree_tsqr": [_vp, _i64, _vp, _vp],
+    "candmc_tau_recon": [ctypes.c_char, _i64, _i64, _i64, _vp, _vp, _vp],
     "candmc_construct_Q1": [_vp, _i64, _vp, _vp, _i64, _i64, _i64, _i64, _vp],
     "candmc_apply_tsqr_QT": [_vp, _i64, _vp, _vp, _i64, _i64, _i64, _i64, _vp],
     "candmc_compute_invT_from_W": [_vp, _i64, _vp, _vp],

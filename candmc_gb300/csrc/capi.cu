@@ -754,6 +754,50 @@ int candmc_apply_tsqr_QT(const double* Y, int64_t ldy, const double* tau, double
   return apply_qt(Y, ldy, m, (int)b, t.d(), b, B, ldb, k, CANDMC_PREC_FP64, s);
 }
 
+// tau_i = 2 / (1 + ||y_i||^2) over the structure's part of column i (0 when
+// that gives 2, an empty reflector), one warp per column; the norm is a
+// scaled sum of squares (max |y| first), as LAPACK's Frobenius norm scales.
+__global__ void k_tau_recon(char structure, int64_t ncol, int64_t nrow, int64_t lda, const double* Y,
+                            double* tau) {
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= ncol) return;
+  int64_t r0 = 0, r1 = nrow;
+  if (structure == 'L') r0 = i + 1;
+  if (structure == 'U') r1 = i + 1;
+  const double* y = Y + i * lda;
+  double mx = 0.0;
+  for (int64_t r = r0 + lane; r < r1; r += 32) mx = fmax(mx, fabs(y[r]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  double ss = 0.0;
+  if (mx > 0.0)
+    for (int64_t r = r0 + lane; r < r1; r += 32) {
+      const double t = y[r] / mx;
+      ss = fma(t, t, ss);
+    }
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  if (lane == 0) {
+    const double nrm = mx * sqrt(ss);
+    const double t = 2.0 / (nrm * nrm + 1.0);
+    tau[i] = (t == 2.0) ? 0.0 : t;
+  }
+}
+
+int candmc_tau_recon(char structure, int64_t ncol, int64_t nrow, int64_t lda, const double* Y, double* tau,
+                     void* stream) {
+  if ((structure != 'R' && structure != 'L' && structure != 'U') || ncol < 0 || nrow < 0 || !tau ||
+      (ncol > 0 && (!Y || lda < std::max<int64_t>(nrow, 1))))
+    return set_error(CANDMC_ERR_ARG, "tau_recon args");
+  if (ncol == 0) return CANDMC_OK;
+  cudaStream_t s = STREAM(stream);
+  {
+    ProfScope ps(CANDMC_KCLASS_SMALL, 8.0 * ncol * nrow, s);
+    k_tau_recon<<<(unsigned)((ncol * 32 + 255) / 256), 256, 0, s>>>(structure, ncol, nrow, lda, Y, tau);
+  }
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
 int candmc_compute_invT_from_W(const double* W, int64_t b, double* invT, void* stream) {
   if (!W || !invT || b < 1) return set_error(CANDMC_ERR_ARG, "compute_invT_from_W args");
   cudaStream_t s = STREAM(stream);

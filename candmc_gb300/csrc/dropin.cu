@@ -140,6 +140,18 @@ void apply_tsqr_QT(double const* Y, int64_t const lda_Y, double const* tau, doub
 }
 
 // ------------------------------------------------------------------ reconstruction
+void tau_recon(const char structure, const int ncol, const int nrow, const int lda, double const* Y,
+               double* tau) {
+  if (ncol <= 0) return;
+  DMat dY, dt;
+  if (!stage(dY, Y, lda, nrow, ncol) || !dt.alloc(ncol, 1)) {
+    g_status = CANDMC_ERR_ALLOC;
+    return;
+  }
+  int rc = candmc_tau_recon(structure, ncol, nrow, dY.ld, dY.p, dt.p, nullptr);
+  if (finish(rc) == CANDMC_OK) dt.out(tau, ncol);
+}
+
 void compute_invT_from_W(double const* W, int64_t b, double* invT) {
   DMat dW, dX;
   if (!stage(dW, W, b, b, b) || !stage(dX, invT, b, b, b)) { g_status = CANDMC_ERR_ALLOC; return; }

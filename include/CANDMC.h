@@ -19,6 +19,9 @@
 /* 2D QR with Yamamoto's basis-kernel representation for full matrices */
 #include "candmc/qr_y2d.h"
 
+/* tau from Householder vectors (the reference's alg/shared/util.h) */
+#include "candmc/util.h"
+
 /* the C ABI underneath */
 #include "candmc_gb300.h"
 

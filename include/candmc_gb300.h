@@ -131,6 +131,15 @@ int candmc_construct_Q1(const double* Y, int64_t ldy, const double* tau, double*
 int candmc_apply_tsqr_QT(const double* Y, int64_t ldy, const double* tau, double* B, int64_t ldb,
                          int64_t m, int64_t b, int64_t k, void* stream);
 
+/* tau_recon: alg/shared/util.h:675-680 (util.cxx:437-466).  tau (ncol) from
+ * the Householder vectors in Y (nrow x ncol, ld lda): tau_i = 2/(1 + ||y_i||^2),
+ * the norm over column i's part given by structure -- 'R' all nrow rows, 'L'
+ * rows below the diagonal (unit diagonal implicit), 'U' rows 0..i -- and 0 where
+ * that gives 2 (an empty reflector), as the reference does.  Valid for the
+ * exact reflectors of a Householder reconstruction (tau = 2/(y^T y)). */
+int candmc_tau_recon(char structure, int64_t ncol, int64_t nrow, int64_t lda, const double* Y, double* tau,
+                     void* stream);
+
 /* compute_invT_from_W: alg/QR/hh_recon/hh_recon.h:13-15 (hh_recon.cxx:26-31).
  * invT (b x b, ld b) holds Y1 on entry and T^-T = -W^-T*Y1 on return. */
 int candmc_compute_invT_from_W(const double* W, int64_t b, double* invT, void* stream);

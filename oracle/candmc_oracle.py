@@ -331,6 +331,21 @@ def ls_solve(A, B, b):
     return X
 
 
+def tau_recon(structure, Y, nrow=None):
+    """tau_recon (alg/shared/util.cxx:437-466): tau_i = 2/(1 + ||y_i||^2) over
+    column i's part -- 'R' rows 0..nrow-1, 'L' rows i+1..nrow-1, 'U' rows
+    0..i -- mapped to 0 where it equals 2."""
+    Y = np.asarray(Y)
+    nrow = Y.shape[0] if nrow is None else nrow
+    tau = np.zeros(Y.shape[1])
+    for i in range(Y.shape[1]):
+        lo, hi = {"R": (0, nrow), "L": (i + 1, nrow), "U": (0, i + 1)}[structure]
+        nrm = np.linalg.norm(Y[lo:hi, i])
+        t = 2.0 / (nrm * nrm + 1.0)
+        tau[i] = 0.0 if t == 2.0 else t
+    return tau
+
+
 def tau_recon_lower(Y, b, lapack_zero=False):
     """tau_i = 2/(1 + ||Y[i+1:, i]||^2) (alg/shared/util.cxx:437-466, 'L').
 

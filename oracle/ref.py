@@ -10,6 +10,7 @@ present at build time: `available()` says whether it can be used.
 Reference entry points wrapped (file:line of their declarations):
   tree_tsqr, local_tsqr, bitree_tsqr, construct_Q1, apply_tsqr_QT
                                       alg/QR/tsqr/bitree_tsqr.h:16-138
+  tau_recon                           alg/shared/util.h:675-680
   signed_NLU, recursive_NLU, compute_invT_from_W, hh_recon_qr
                                       alg/QR/hh_recon/hh_recon.h:13-75
   Yamamoto                            alg/QR/hh_recon/yamamoto.h
@@ -34,6 +35,7 @@ _SIGS = {
     "ref_bitree_tsqr": [_P, _I, _P, _P, _I, _I, _I, _P],
     "ref_construct_Q1": [_P, _I, _P, _P, _I, _I, _I, _I, _P],
     "ref_apply_tsqr_QT": [_P, _I, _P, _P, _I, _I, _I, _I, _P],
+    "ref_tau_recon": [ctypes.c_char, _I, _I, _I, _P, _P],
     "ref_compute_invT_from_W": [_P, _I, _P],
     "ref_signed_NLU": [_P, _P, _I, _I, _I, _P],
     "ref_recursive_NLU": [_P, _P, _I, _I, _I, _P],
@@ -116,6 +118,15 @@ def apply_tsqr_QT(Y, tau, B, b):
     tau = np.ascontiguousarray(tau, dtype=np.float64)
     lib().ref_apply_tsqr_QT(_p(Y), Y.shape[0], _p(tau), _p(B), m, m, b, k, None)
     return B
+
+
+def tau_recon(structure, Y, nrow=None):
+    """util.cxx:437-466: tau from Householder vectors ('R', 'L' or 'U')."""
+    Y = _f(Y)
+    rows, ncol = Y.shape
+    tau = np.zeros(ncol)
+    lib().ref_tau_recon(structure.encode(), ncol, rows if nrow is None else nrow, rows, _p(Y), _p(tau))
+    return tau
 
 
 # ---- alg/QR/hh_recon

@@ -70,6 +70,11 @@ void ref_apply_tsqr_QT(const double* Y, int64_t ldY, const double* tau, double* 
   apply_tsqr_QT(Y, ldY, tau, B, ldB, m, b, k, 0, 1, 0, one_rank(), tree_data);
 }
 
+// util.h:675-680 (util.cxx:437-466)
+void ref_tau_recon(char structure, int64_t ncol, int64_t nrow, int64_t lda, const double* Y, double* tau) {
+  tau_recon(structure, (int)ncol, (int)nrow, (int)lda, Y, tau);
+}
+
 // hh_recon.h:13-15
 void ref_compute_invT_from_W(const double* W, int64_t b, double* invT) { compute_invT_from_W(W, b, invT); }
 

@@ -11,6 +11,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "CANDMC.h"
@@ -170,6 +171,42 @@ int main() {
     const bool n_ok = agg.n == k;
     fails += report(n_ok ? "aggregator ||A + aQm aT aQm^T A - R||/||A||" : "aggregator count wrong",
                     n_ok ? sqrt(num / den) : 1.0, 1e-13);
+  }
+  // tree_tsqr (dtpqrt's contract): [R1; R2] from the fixture's upper triangles
+  // with the fixture's values left below them; R over R1's triangle, V over
+  // R2's, nothing else written.  R*R^T-independent check: R^T R = R1^T R1 + R2^T R2.
+  {
+    const int64_t b = 21;
+    std::vector<double> A(2 * b * b), A0;
+    for (int64_t c = 0; c < b; ++c)
+      for (int64_t r = 0; r < 2 * b; ++r) A[c * 2 * b + r] = fixture(r, c, 2 * b, 0.5);
+    A0 = A;
+    std::vector<double> buf(2 * b * b), T(16 * b, -7.0);
+    tree_tsqr(A.data(), buf.data(), b, T.data());
+    bool lower_ok = true;
+    double num = 0, den = 0;
+    for (int64_t c = 0; c < b; ++c) {
+      for (int64_t r = 0; r < b; ++r)
+        if (r > c) lower_ok = lower_ok && A[c * 2 * b + r] == A0[c * 2 * b + r] &&
+                              A[c * 2 * b + b + r] == A0[c * 2 * b + b + r];
+      for (int64_t d = 0; d < b; ++d) {   // (R^T R - R1^T R1 - R2^T R2)(c, d)
+        double g = 0, g0 = 0;
+        for (int64_t r = 0; r <= std::min(c, d); ++r) {
+          g += A[c * 2 * b + r] * A[d * 2 * b + r];
+          g0 += A0[c * 2 * b + r] * A0[d * 2 * b + r] + A0[c * 2 * b + b + r] * A0[d * 2 * b + b + r];
+        }
+        num += (g - g0) * (g - g0);
+        den += g0 * g0;
+      }
+    }
+    fails += report(lower_ok ? "tree_tsqr ||R^TR - R1^TR1 - R2^TR2||/||.||" : "tree_tsqr wrote below a diagonal",
+                    lower_ok ? sqrt(num / den) : 1.0, 1e-13);
+    // tau_recon('U') of the V block gives the node reflectors' tau = T's diagonal
+    std::vector<double> tau(b);
+    tau_recon('U', (int)b, (int)b, (int)(2 * b), A.data() + b, tau.data());
+    double tdiff = 0;
+    for (int64_t c = 0; c < b; ++c) tdiff = std::max(tdiff, fabs(tau[c] - T[c * 16 + (c % 16)]));
+    fails += report("tree_tsqr T diagonal vs tau_recon('U')", tdiff, 1e-13);
   }
   // a grid larger than 1 x 1 is rejected without touching the data
   {

@@ -16,6 +16,7 @@ Cases (key prefix -> reference function):
   c2/{A,YR}             QR_2D_pipe of a 256 x 256 U diag(logspace(0,-6)) V^T, b = 128
   tree/<b>/{in,out,T}   tree_tsqr (dtpqrt)   alg/QR/tsqr/bitree_tsqr.cxx:20-34
   tsqr/{YR,R,tau,Q1,QtB} bitree_tsqr, construct_Q1, apply_tsqr_QT (one rank)
+  tau/{L,U,R}           tau_recon            alg/shared/util.cxx:437-466
   yam/{A,Qm,W}          Yamamoto             alg/QR/hh_recon/yamamoto.cxx:98-174
   invT/{fromW,fromY,fromY2}                  hh_recon.cxx:26-31, qr_2d.cxx:22-106
   upd/{W,noW}           upd_A with T from W and from Y^T Y   qr_2d.cxx:224-282
@@ -94,6 +95,10 @@ def main():
     out["tsqr/YR"], out["tsqr/R"], out["tsqr/tau"] = YRt, R, tau
     out["tsqr/Q1"] = ref.construct_Q1(YRt, tau, 32)
     out["tsqr/QtB"] = ref.apply_tsqr_QT(YRt, tau, gaussian(256, 8, 401), 32)
+    YRh, _ = ref.hh_recon_qr(gaussian(256, 32, 406), 32)
+    out["tau/L"] = ref.tau_recon("L", YRh)
+    out["tau/U"] = ref.tau_recon("U", np.triu(out["tree/32/out"][32:]))
+    out["tau/R"] = ref.tau_recon("R", YRh[32:])
     A2, Qm, Wy = ref.Yamamoto(gaussian(256, 32, 402), 32)
     out["yam/A"], out["yam/Qm"], out["yam/W"] = A2, Qm, Wy
     YRh, Wh = ref.hh_recon_qr(gaussian(256, 32, 403), 32)

@@ -157,6 +157,18 @@ def test_single_rank_tsqr_is_the_reference(cm, rg):
     close(host(dB), rg["tsqr/QtB"], 32)
 
 
+def test_tau_recon_is_the_reference(cm, rg):
+    """tau_recon's three structures (util.cxx:437-466)."""
+    dA = dev(fx.gaussian(256, 32, 406))
+    cm.hh_recon_qr(dA)
+    YRh = host(dA)
+    close(cm.tau_recon("L", dA).cpu().numpy(), rg["tau/L"], 32)
+    close(cm.tau_recon("U", dev(np.triu(rg["tree/32/out"][32:]))).cpu().numpy(), rg["tau/U"], 32)
+    close(cm.tau_recon("R", dev(YRh[32:])).cpu().numpy(), rg["tau/R"], 32)
+    # an empty reflector maps to 0, as in the reference
+    assert cm.tau_recon("L", dev(np.eye(4))).cpu().numpy().tolist() == [0.0, 0.0, 0.0, 0.0]
+
+
 def test_yamamoto_is_the_reference(cm, rg):
     """The pair equals the reference's up to the reference's column signs d:
     Qm = Qm_ref d, W = d W_ref d, and the panel's Y\\(S R) is the same."""

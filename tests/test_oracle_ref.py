@@ -108,6 +108,14 @@ def test_single_rank_tsqr_oracle_is_the_reference(rg):
     close(co.apply_tsqr_QT(YR, tau, B, 32), rg["tsqr/QtB"], 32)
 
 
+def test_tau_recon_oracle_is_the_reference(rg):
+    YRh, _ = co.hh_recon_qr(fx.gaussian(256, 32, 406), 32)
+    close(co.tau_recon("L", YRh), rg["tau/L"], 32)
+    close(co.tau_recon("U", np.triu(rg["tree/32/out"][32:])), rg["tau/U"], 32)
+    close(co.tau_recon("R", YRh[32:]), rg["tau/R"], 32)
+    close(co.tau_recon_lower(lp.unit_lower(YRh, 32), 32, lapack_zero=True), rg["tau/L"], 32)
+
+
 def test_yamamoto_oracle_is_the_reference(rg):
     A = fx.gaussian(256, 32, 402)
     YR, Qm, W, s = yo.Yamamoto(A, 32)
