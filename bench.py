@@ -11,7 +11,11 @@ A -= Y T^T (Y^T A).  One step = restore A from the device-resident input
 (2 GiB D2D copy) + one full factorization; the 2 GiB input is larger than L2
 (129 MB), so no flush is needed between steps.  Metric: FP64-equivalent
 TFLOP/s = (4/3 n^3) / step time (the reference's GFlops formula
-2mk^2 - 2/3 k^3 at m = k, bench/QR/bench_qr_2d.cxx:85-87).
+2mk^2 - 2/3 k^3 at m = k, bench/QR/bench_qr_2d.cxx:85-87).  The line also
+carries the whole-matrix backward error and orthogonality of the timed
+factorization, and, each with its own step count, `fp64_form` (the plain FP64
+form on the same matrix), `tsqr_hr` (the TSQR-HR panel workload below) and
+`forms` (the precision-form workload below).
 
 Other workloads (`--workload`), one JSON line each in the same format:
   tsqr_hr  TSQR-HR of one 8192 x 64 N(0,1) panel (seed 0): hh_recon_qr,
@@ -32,8 +36,11 @@ Other workloads (`--workload`), one JSON line each in the same format:
 
 N > 1 (torchrun) runs N independent replicas (the problems are not sharded
 across GPUs), value = N * work / max time.  `--impl reference` times the
-reference's own single-rank call sequence (dgeqrf, dorgqr, signed LU, dtrsm,
-dgemm: oracle/reference_lapack.py) on the host cores on a bounded sample.
+reference's own CPU path on the host cores: for caqr, full QR_2D
+factorizations of the same n = 16384 matrix (the compiled reference where it
+was built from its sources, oracle/_ref; elsewhere its LAPACK call sequence
+replayed on the same OpenBLAS, oracle/reference_lapack.py, which gives
+bitwise-equal results); its warm-up steps factor a leading block only.
 """
 import argparse
 import json
@@ -64,7 +71,7 @@ def parse():
     p.add_argument("--n", type=int, default=None)
     p.add_argument("--b", type=int, default=None)
     p.add_argument("--form", choices=["fp64", "ozaki", "fp32"], default=None)
-    p.add_argument("--forms", default="ozaki,fp32,fp64")
+    p.add_argument("--forms", default="ozaki,fp32")
     p.add_argument("--entry", choices=["pipe", "qr2d"], default="pipe",
                    help="QR_2D_pipe (lookahead, the reference tests' default) or QR_2D")
     p.add_argument("--sigma-min", type=float, default=1e-6)
@@ -78,8 +85,18 @@ def parse():
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-extra", action="store_true",
+                   help="caqr: skip the fp64-form, TSQR-HR and precision-form legs")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     return p.parse_args()
+
+
+_T0 = time.time()
+
+
+def log(msg):
+    """Progress on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.time() - _T0:7.1f}s] {msg}", file=sys.stderr, flush=True)
 
 
 def flops(n):
@@ -202,23 +219,41 @@ def measured_peaks():
     return json.load(open(path)) if os.path.exists(path) else {}
 
 
-def sampled_backward_error(cm, A0, YR, b, ncols=64, seed=0):
-    """||Q^T A0[:, S] - R[:, S]||_F / ||A0[:, S]||_F over a random column sample S.
+def full_accuracy(cm, A0, YR, b, precision="fp64", cols=None, orth_cols=None, seed=0):
+    """Backward error ||Q^T A0 - R||_F / ||A0||_F and orthogonality
+    ||Q Q^T - I||_F of the factor held in YR, computed on the GPU.
 
-    Q^T is applied panel by panel with update_A (T from Y^T Y, qr_2d.cxx:22-60),
-    the reference tests' residual restricted to sampled columns.
+    Q^T is applied panel by panel with update_A (T from Y^T Y, qr_2d.cxx:22-60)
+    to [E | A0], E holding unit vectors, in the given arithmetic form: that
+    gives rows of Q explicitly and Q^T A0 at once (the reference tests' two
+    criteria, test_qr_2d.cxx:285-301 and test_bitree_tsqr.cxx:370-427).  By
+    default over every column of A0 and every row of Q; with cols / orth_cols,
+    over that many sampled columns of A0 / rows of Q (the Gram block of the
+    sampled rows against I).  Q Q^T is formed in FP64.
     """
     import torch
     m, n = YR.shape
     rng = np.random.default_rng(seed)
-    S = torch.from_numpy(np.sort(rng.choice(n, size=min(ncols, n), replace=False))).to(A0.device)
-    X = A0[:, S].t().contiguous().t()
-    for r0 in range(0, n, b):
+    qrows = np.arange(m) if orth_cols is None else np.sort(rng.choice(m, size=orth_cols, replace=False))
+    acols = np.arange(n) if cols is None else np.sort(rng.choice(n, size=cols, replace=False))
+    nq, na = len(qrows), len(acols)
+    dev_ = A0.device
+    X = torch.zeros((nq + na, m), dtype=torch.float64, device=dev_).t()
+    X[torch.from_numpy(qrows).to(dev_), torch.arange(nq, device=dev_)] = 1.0
+    ac = torch.from_numpy(acols).to(dev_)
+    X[:, nq:] = A0[:, ac]
+    for r0 in range(0, min(m, n), b):
         bb = min(b, n - r0)
-        cm.update_A(YR[r0:, r0:r0 + bb], X[r0:, :], bb, None)
-    R = torch.triu(YR)[:, S]
+        cm.update_A(YR[r0:, r0:r0 + bb], X[r0:, :], bb, None, precision=precision)
+    R = torch.triu(YR)[:, ac]
+    bwd = float(torch.linalg.norm(X[:, nq:] - R) / torch.linalg.norm(A0[:, ac]))
+    Qc = X[:, :nq]                      # Q^T e_j = row j of Q, as columns
+    G = Qc.t() @ Qc
+    G.diagonal().sub_(1.0)
+    orth = float(torch.linalg.norm(G))
+    del X, G
     torch.cuda.synchronize()
-    return float(torch.linalg.norm(X - R) / torch.linalg.norm(A0[:, S]))
+    return bwd, orth
 
 
 class Ctx:
@@ -387,19 +422,22 @@ def cpu_ls_rate(tasks, seconds):
     return done / (total / cores), done, cores
 
 
-def cpu_caqr(args, n):
+def cpu_caqr_sample(A0h, b):
+    """One full factorization of the same matrix by the reference's CPU path:
+    the compiled reference (oracle/_ref) where it was built, else its LAPACK
+    call sequence replayed on the same OpenBLAS (bitwise-equal to it;
+    tests/test_oracle_ref.py).  Returns (seconds, kind, threads)."""
+    from oracle import ref
     from oracle import reference_lapack as rl
-    rng = np.random.default_rng(args.seed)
-    A0 = np.asfortranarray(rng.standard_normal((n, n)))
-    rl.QR_2D_lapack(A0.copy(order="F")[: n // 4, : n // 4].copy(order="F"), args.b)  # warm-up
-    A = A0.copy(order="F")
+    A = np.array(A0h, order="F")
     t0 = time.perf_counter()
-    rl.QR_2D_lapack(A, args.b)
-    dt = time.perf_counter() - t0
-    return {"value": flops(n) / dt / 1e12, "unit": "TFLOP/s", "cores": rl.blas_threads(),
-            "kind": "port",
-            "sample": f"reference QR_2D call sequence on LAPACK/BLAS (scipy OpenBLAS), n={n}, "
-                      f"b={args.b}, Gaussian input, one factorization ({dt:.1f} s)"}
+    if ref.available():
+        ref.QR_2D(A, b)
+        kind = "reference"
+    else:
+        rl.QR_2D_lapack(A, b)
+        kind = "port"
+    return time.perf_counter() - t0, kind, rl.blas_threads()
 
 
 def cpu_tsqr_hr(args, m, b, reps=None):
@@ -427,33 +465,29 @@ def run_reference(args):
     line = {"impl": "reference", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "scaling": "weak", "vs_baseline": None, "data": "synthetic", "higher_is_better": True}
     if wl == "caqr":
-        from oracle import fixtures as fx
+        A0 = caqr_input_host(args)
+        from oracle import ref
         from oracle import reference_lapack as rl
-        n = args.ref_n
-        rng = np.random.default_rng(args.seed)
-        A0 = np.asfortranarray(fx.svd_matrix(n, n, args.seed, args.sigma_min)) if n <= 4096 else \
-            np.asfortranarray(rng.standard_normal((n, n)))
+        use_ref = ref.available()
+        nw = max(512, (args.n // 8) // args.b * args.b)
+        for _ in range(args.warmup):      # warm-up: the leading block only (pages in, starts BLAS threads)
+            W = np.array(A0[:nw, :nw], order="F")
+            ref.QR_2D(W, args.b) if use_ref else rl.QR_2D_lapack(W, args.b)
         times = []
-        for it in range(args.warmup + args.steps):
-            A = A0.copy(order="F")
-            t0 = time.perf_counter()
-            rl.QR_2D_lapack(A, args.b)
-            dt = time.perf_counter() - t0
-            if it >= args.warmup:
-                times.append(dt)
+        for _ in range(args.steps):
+            dt, kind, cores = cpu_caqr_sample(A0, args.b)
+            times.append(dt)
+            log(f"reference step {len(times)}: {dt:.1f} s")
         tot = sum(times)
-        val = flops(n) * len(times) / tot / 1e12
-        cores = rl.blas_threads()
+        val = flops(args.n) * len(times) / tot / 1e12
         line.update({
             "metric": "CAQR TFLOP/s (FP64-equivalent, 4/3 n^3 per factorization)",
             "value": val, "unit": "TFLOP/s", "ms_per_step": 1e3 * tot / len(times), "dtype": "f64",
-            "config": {"workload": f"CAQR QR_2D n={args.n} b={args.b} float64 (timed on a bounded "
-                                   f"n={n} sample on the host cores)",
-                       "n": args.n, "b": args.b, "sample_n": n, "form": "reference LAPACK call sequence",
-                       "parallelism": "host BLAS threads"},
-            "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-                             "sample": f"QR_2D_lapack n={n} (bounded sample of the n={args.n} workload; "
-                                       "Gaussian input above n=4096)"}})
+            "config": caqr_config(args),
+            "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": kind,
+                             "sample": f"{len(times)} full QR_2D factorizations of the same n={args.n} matrix "
+                                       f"({'compiled reference' if kind == 'reference' else 'the reference call sequence replayed on the same OpenBLAS, bitwise-equal to the compiled reference'}); "
+                                       f"warm-up steps factor the leading {nw} x {nw} block"}})
     elif wl == "tsqr_hr":
         gf, reps, cores = cpu_tsqr_hr(args, args.m, args.b, reps=args.warmup + args.steps)
         line.update({"metric": "TSQR-HR GFLOP/s (2mb^2 - 2/3 b^3 per panel)", "value": gf,
@@ -487,24 +521,60 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------- caqr (default)
+def caqr_config(args):
+    """The workload, identical in both arms (this one and --impl reference)."""
+    return {"workload": f"CAQR n={args.n} b={args.b} float64, A=U diag(logspace(0,"
+                        f"{np.log10(args.sigma_min):.0f},n)) V^T, U,V Haar (PCG64 seed {args.seed}, "
+                        "QR of the Gaussian draws on the GPU)",
+            "n": args.n, "b": args.b, "seed": args.seed, "sigma_min": args.sigma_min,
+            "l2": f"input {8.0 * args.n * args.n / 2**30:.1f} GiB "
+                  + ("> L2 129 MB, no flush needed" if 8.0 * args.n * args.n > 129e6 else "(< L2)")}
+
+
+def caqr_input_host(args):
+    """The benchmark matrix as a Fortran-ordered host array: the same bytes
+    the GPU arm factors (generated on the GPU when one is present)."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            A0, _ = make_input_gpu(args.n, args.seed, args.sigma_min, torch.device("cuda", 0))
+            h = np.asfortranarray(A0.cpu().numpy())
+            del A0
+            torch.cuda.empty_cache()
+            return h
+    except ImportError:
+        pass
+    from oracle import fixtures as fx
+    return np.asfortranarray(fx.svd_matrix(args.n, args.n, args.seed, args.sigma_min))
+
+
+def caqr_form_run(ctx, A0, A, b, form, entry, steps, warmup):
+    """warm-up + timed factorizations of A0 (restored into A each step) in one form."""
+    import torch
+    cm = ctx.cm
+    qr = cm.QR_2D_pipe if entry == "pipe" else cm.QR_2D
+
+    def step():
+        A.copy_(A0)
+        qr(A, b, precision=form)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    dom = {"fp64": ["gemm_tn", "gemm_nn"], "ozaki": ["oz_tn", "oz_nn"], "fp32": ["f32"]}[form]
+    t_max, launches, prof, clk = ctx.timed(step, steps, dom)
+    return step, dom, t_max, launches, prof, clk
+
+
 def wl_caqr(args, ctx):
     import torch
-    cm, lib = ctx.cm, ctx.lib
+    cm = ctx.cm
     n, b, prec = args.n, args.b, args.form
     A0, _ = make_input_gpu(n, args.seed + ctx.rank * 1000 if ctx.world > 1 else args.seed,
                            args.sigma_min, ctx.dev)
     A = torch.empty_like(A0.t()).t()
-    qr = cm.QR_2D_pipe if args.entry == "pipe" else cm.QR_2D
-
-    def step():
-        A.copy_(A0)
-        qr(A, b, precision=prec)
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    dom = {"fp64": ["gemm_tn", "gemm_nn"], "ozaki": ["oz_tn", "oz_nn"], "fp32": ["f32"]}[prec]
-    t_max, launches, prof, clk = ctx.timed(step, args.steps, dom)
+    step, dom, t_max, launches, prof, clk = caqr_form_run(ctx, A0, A, b, prec, args.entry, args.steps,
+                                                          args.warmup)
     value = ctx.world * flops(n) * args.steps / (t_max / 1e3) / 1e12
     dom_ms = sum(prof[c][0] for c in dom)
     dom_work = sum(prof[c][1] for c in dom)
@@ -534,10 +604,16 @@ def wl_caqr(args, ctx):
         roof = fp64_roof(prof, dom, "k_gemm_f64 (Y^T A split-K partials and A -= Y Z)", t_max)
         roof["traffic"] = traffic_from_profile("gemm_f64_caqr_n16384.md")
 
+    log(f"caqr {prec}: {t_max / args.steps:.1f} ms/step")
     shares = kernel_time_shares(ctx, step)
     roof["share_of_kernel_time"] = sum(shares.get(c, 0.0) for c in dom)
-    bwd = sampled_backward_error(cm, A0, A, b)
+    # accuracy of the last timed factorization, over the whole matrix, checked in FP64
+    bwd, orth = full_accuracy(cm, A0, A, b, precision="fp64")
+    accuracy = {"backward_error": bwd, "orthogonality": orth, "bound": 1e-13,
+                "how": "||Q^T A - R||_F/||A||_F and ||Q Q^T - I||_F over the whole matrix; Q^T applied "
+                       "to [I | A] panel by panel in FP64 on the GPU, Q Q^T formed in FP64"}
 
+    log(f"caqr accuracy: backward {bwd:.2e}, orthogonality {orth:.2e}")
     e2e = None
     if not args.no_e2e:
         src = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
@@ -553,23 +629,52 @@ def wl_caqr(args, ctx):
             if it >= 1:
                 tt += dt
         e2e = {"value": ctx.world * flops(n) * args.steps / tt / 1e12, "unit": "TFLOP/s",
-               "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n}
+               "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n,
+               "entry": "candmc_QR_2D_host (host pointers: copy in, lookahead factorization, copy out)"}
+        del src, work
 
-    cpu = cpu_caqr(args, min(args.ref_n, n)) if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu \
-        else None
+    log("caqr e2e done")
+    extra = {}
+    if not args.no_extra and ctx.world == 1:
+        extra["fp64_form"] = caqr_fp64_leg(args, ctx, A0, A)
+        log("fp64 form leg done")
+        extra["tsqr_hr"] = tsqr_hr_leg(args, ctx)
+        log("tsqr_hr leg done")
+        extra["forms"] = forms_leg(args, ctx)
+        log("forms leg done")
+
+    cpu = None
+    if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu:
+        A0h = np.asfortranarray(A0.cpu().numpy())
+        dt, kind, cores = cpu_caqr_sample(A0h, b)
+        cpu = {"value": flops(n) / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": kind,
+               "sample": f"one full QR_2D factorization of the same n={n} matrix ({dt:.1f} s; "
+                         + ("compiled reference" if kind == "reference" else
+                            "the reference's LAPACK call sequence replayed on the same OpenBLAS, "
+                            "bitwise-equal to the compiled reference") + ")"}
+        del A0h
+        log("cpu baseline done")
     dtype = {"fp64": "f64", "ozaki": "f64 (emulated: bf16 Ozaki slices, fp32 accumulate)",
              "fp32": "f64 panels, fp32 trailing-update contractions"}[prec]
     line = base_line(args, ctx, "CAQR TFLOP/s (FP64-equivalent, 4/3 n^3 per factorization)", value,
-                     "TFLOP/s", t_max / args.steps, dtype,
-                     {"workload": f"CAQR QR_2D n={n} b={b} float64, A=U diag(logspace(0,"
-                                  f"{np.log10(args.sigma_min):.0f},n)) V^T, U,V Haar (PCG64 seed {args.seed})",
-                      "n": n, "b": b, "form": prec, "entry": args.entry,
-                      "parallelism": f"replicas x{ctx.world}",
-                      "l2": "input 2 GiB > L2 129 MB, no flush needed"})
-    line.update({"clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof,
-                 "cpu_baseline": cpu,
-                 "accuracy": {"backward_error_sampled": bwd, "columns": 64, "bound": 1e-13}})
+                     "TFLOP/s", t_max / args.steps, dtype, caqr_config(args))
+    line.update({"variant": {"form": prec, "entry": "QR_2D_pipe" if args.entry == "pipe" else "QR_2D",
+                             "parallelism": f"replicas x{ctx.world}"},
+                 "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof,
+                 "cpu_baseline": cpu, "accuracy": accuracy})
+    line.update(extra)
     return line
+
+
+def caqr_fp64_leg(args, ctx, A0, A, steps=2, warmup=1):
+    """The plain FP64 form on the same matrix: TFLOP/s and accuracy."""
+    _, dom, t_max, launches, prof, clk = caqr_form_run(ctx, A0, A, args.b, "fp64", args.entry, steps, warmup)
+    roof = fp64_roof(prof, dom, "k_gemm_f64", t_max)
+    bwd, orth = full_accuracy(ctx.cm, A0, A, args.b, precision="fp64")
+    return {"value": flops(args.n) * steps / (t_max / 1e3) / 1e12, "unit": "TFLOP/s", "steps": steps,
+            "warmup": warmup, "ms_per_step": t_max / steps, "gpu_launches": launches,
+            "dominant_kernel_fp64_frac": roof["frac"], "clocks": clk,
+            "accuracy": {"backward_error": bwd, "orthogonality": orth, "how": "as the headline's"}}
 
 
 # ----------------------------------------------------------------- tsqr_hr
@@ -675,20 +780,16 @@ def wl_forms(args, ctx):
         s = torch.logspace(0, np.log10(smin), n, dtype=torch.float64, device=ctx.dev)
         A0 = cm.colmajor((U * s[None, :]) @ V.t())
         A = torch.empty_like(A0.t()).t()
-        x64 = None
-        for form in sorted(forms, key=lambda f: f != "fp64"):
-            def step():
-                A.copy_(A0)
-                cm.QR_2D_pipe(A, b, precision=form)
-            for _ in range(args.warmup):
-                step()
-            torch.cuda.synchronize()
-            dom = {"fp64": ["gemm_tn", "gemm_nn"], "ozaki": ["oz_tn", "oz_nn"], "fp32": ["f32"]}[form]
-            t_max, launches, prof, clk = ctx.timed(step, args.steps, dom)
+        # the FP64 oracle of the least-squares solutions: the plain FP64 form
+        x64, st64 = cm.ls_solve(A0, B, b, precision="fp64", max_refine=20)
+        r64 = float(torch.linalg.norm(B - A0 @ x64))
+        for form in forms:
+            _, dom, t_max, launches, prof, clk = caqr_form_run(ctx, A0, A, b, form, "pipe", args.steps,
+                                                               args.warmup)
             total_launches += launches
             clk_all.append(clk)
             tf = qr_flops(m, n) * args.steps / (t_max / 1e3) / 1e12
-            bwd = sampled_backward_error(cm, A0, A, b)
+            bwd, orth = full_accuracy(cm, A0, A, b, precision="fp64", cols=256, orth_cols=256)
             dom_ms = sum(prof[c][0] for c in dom)
             dom_tf = sum(prof[c][1] for c in dom) / (dom_ms / 1e3) / 1e12 if dom_ms else None
             # least squares, 16 right-hand sides, FP64 refinement
@@ -701,21 +802,18 @@ def wl_forms(args, ctx):
             ls_ms = e0.elapsed_time(e1)
             Rr = B - A0 @ X
             opt = float(torch.linalg.norm(A0.t() @ Rr) / (torch.linalg.norm(A0) * torch.linalg.norm(Rr)))
-            if form == "fp64":
-                x64 = X.clone()
-                r64 = float(torch.linalg.norm(Rr))
             rec = {"sigma_min": smin, "form": form, "qr_tflops": tf, "qr_ms": t_max / args.steps,
-                   "dominant_kernel_tflops": dom_tf, "backward_error_sampled": bwd, "ls_ms": ls_ms,
-                   "refine_steps": st["steps"], "last_correction": st["last_change"],
-                   "normal_eq_residual": opt}
-            if x64 is not None:
-                rec["x_rel_diff_vs_fp64"] = float(torch.linalg.norm(X - x64) / torch.linalg.norm(x64))
-                rec["resid_rel_diff_vs_fp64"] = abs(float(torch.linalg.norm(Rr)) - r64) / r64
+                   "dominant_kernel_tflops": dom_tf, "backward_error_256_cols": bwd,
+                   "orthogonality_256_rows": orth,
+                   "ls_ms": ls_ms, "refine_steps": st["steps"], "last_correction": st["last_change"],
+                   "normal_eq_residual": opt,
+                   "x_rel_diff_vs_fp64": float(torch.linalg.norm(X - x64) / torch.linalg.norm(x64)),
+                   "resid_rel_diff_vs_fp64": abs(float(torch.linalg.norm(Rr)) - r64) / r64}
             cases.append(rec)
             if smin == 1e-10 and form == forms[0]:
                 head = (tf, t_max / args.steps, form, prof, dom)
             del X, Rr
-        del A0, A
+        del A0, A, x64
     tf, ms, form, prof, dom = head
     roof = None
     if form == "ozaki":
@@ -732,8 +830,36 @@ def wl_forms(args, ctx):
                       "m": m, "n": n, "b": b, "forms": forms, "headline": f"{form} at sigma_min 1e-10",
                       "l2": "input 4 GiB > L2"})
     line.update({"clocks": clk_all[0] if clk_all else None, "clocks_all": clk_all, "e2e": None,
-                 "gpu_launches": total_launches, "roofline": roof, "cpu_baseline": None, "cases": cases})
+                 "gpu_launches": total_launches, "roofline": roof, "cpu_baseline": None, "cases": cases,
+                 "accuracy_how": "backward error ||Q^T A_S - R_S||_F/||A_S||_F over 256 sampled columns S "
+                                 "and ||(Q Q^T - I)_RR||_F over 256 sampled rows R, Q^T applied in FP64; "
+                                 "LS errors against the plain FP64 form's solution"})
     return line
+
+
+def _sub_args(args, **kw):
+    import copy
+    a = copy.copy(args)
+    for k, v in kw.items():
+        setattr(a, k, v)
+    return a
+
+
+def tsqr_hr_leg(args, ctx):
+    """TSQR-HR of the 8192 x 64 N(0,1) seed-0 panel, as `--workload tsqr_hr`."""
+    a = _sub_args(args, m=8192, b=64, seed=0, steps=20, warmup=5, no_e2e=True, cpu_seconds=5.0)
+    ln = wl_tsqr_hr(a, ctx)
+    return {k: ln[k] for k in ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config",
+                               "roofline", "accuracy", "cpu_baseline", "clocks", "gpu_launches")}
+
+
+def forms_leg(args, ctx):
+    """The precision forms at m = 32768, n = 16384 (seed 2), as `--workload forms`
+    with two timed steps per form."""
+    a = _sub_args(args, m=32768, n=16384, b=128, seed=2, steps=2, warmup=1, forms="ozaki,fp32")
+    ln = wl_forms(a, ctx)
+    return {k: ln[k] for k in ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config",
+                               "roofline", "cases", "accuracy_how", "clocks", "gpu_launches")}
 
 
 # ----------------------------------------------------------------- batched
@@ -966,7 +1092,7 @@ def wl_serve(args, ctx):
 DEFAULTS = {
     "caqr": {"n": 16384, "b": 128, "form": "ozaki", "seed": 1},
     "tsqr_hr": {"m": 8192, "b": 64, "seed": 0},
-    "forms": {"m": 32768, "n": 16384, "b": 128, "seed": 2, "form": "ozaki"},
+    "forms": {"m": 32768, "n": 16384, "b": 128, "seed": 2, "form": "ozaki"},  # --forms ozaki,fp32
     "batched": {"count": 4096, "seed": 3},
     "serve": {"count": 400, "form": "fp32", "seed": 4},
 }

@@ -175,6 +175,11 @@ extern "C" int candmc_set_tuning(const char* key, int64_t value) {
     g_pipe_leaf_rows = value;
     return CANDMC_OK;
   }
+  if (std::string(key) == "panel_oz_min_rows") {
+    if (value < 0) return set_error(CANDMC_ERR_ARG, "panel_oz_min_rows >= 0 (0 disables)");
+    g_panel_oz_min_rows = value;
+    return CANDMC_OK;
+  }
   if (std::string(key) == "pipe_tree") {
     if (value != 0 && value != 1) return set_error(CANDMC_ERR_ARG, "pipe_tree is 0 or 1");
     g_pipe_tree = (int)value;

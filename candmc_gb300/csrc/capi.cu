@@ -23,6 +23,8 @@ namespace candmc {
 
 static thread_local std::string g_last_error;
 
+int64_t g_panel_oz_min_rows = 2048;
+
 int set_error(int code, const char* what) {
   g_last_error = what ? what : "";
   return code;
@@ -93,8 +95,15 @@ int hr_rec(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, int
   if (b <= kDirectB) return hr_direct4(A, lda, m, b, T, ldT, nullptr, 0, st, s);
   const int b1 = b / 2, b2 = b - b1;
   CANDMC_RET(hr_rec(A, lda, m, b1, T, ldT, st, precision, s));
-  // the panel itself stays in FP64 (its updates are m x b/2 x b/2: small)
-  CANDMC_RET(apply_qt(A, lda, m, b1, T, ldT, A + (int64_t)b1 * lda, lda, b2, CANDMC_PREC_FP64, s));
+  // Q1^T on the right half.  The reflectors, norms, tree and T stay FP64;
+  // this m x b/2 x b/2 product is a trailing update, so in the emulated-FP64
+  // form (and on tall panels, where its FP64 cost is on the panel's critical
+  // path) it runs on the tensor cores with the panel kept in FP64 storage.
+  if (precision == CANDMC_PREC_OZAKI && g_panel_oz_min_rows > 0 && m >= g_panel_oz_min_rows)
+    CANDMC_RET(apply_qt_ozaki(A, lda, kUnitLower, m, b1, mref(T, ldT, 1, kUpper), A + (int64_t)b1 * lda,
+                              lda, b2, m, st, s, true));
+  else
+    CANDMC_RET(apply_qt(A, lda, m, b1, T, ldT, A + (int64_t)b1 * lda, lda, b2, CANDMC_PREC_FP64, s));
   double* T22 = T + (int64_t)b1 * ldT + b1;
   CANDMC_RET(hr_rec(A + (int64_t)b1 * lda + b1, lda, m - b1, b2, T22, ldT, st, precision, s));
   // G = Y1[b1:m, :]^T * Y2   (Y2 unit-lower in A[b1:, b1:])

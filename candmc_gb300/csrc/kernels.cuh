@@ -67,9 +67,14 @@ int larft_from_gram(const double* G, int64_t ldg, const double* tau, int b, doub
 // ozaki.cu: emulated-FP64 trailing update on tcgen05.  C holds df64 pairs
 // (float hi, float lo in each 8-byte slot); rows < fp64_rows are written back
 // as FP64.  Top is the operator T^T applied to Y^T C.
+// With c_fp64, C is FP64 storage (a panel's own columns) instead.
 int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
                    double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
-                   cudaStream_t s);
+                   cudaStream_t s, bool c_fp64 = false);
+// rows from which hr_rec applies a half panel's Q^T to the other half with the
+// emulated-FP64 contraction when the factorization runs in that form (tuning
+// knob "panel_oz_min_rows"; 0 disables)
+extern int64_t g_panel_oz_min_rows;
 // gemm_f32.cu: the same update with FP32 contractions (df64 storage of C).
 int apply_qt_f32(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top, double* C,
                  int64_t ldc, int64_t n, int64_t fp64_rows, cudaStream_t s);

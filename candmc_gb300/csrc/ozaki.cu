@@ -297,6 +297,7 @@ struct OzArgs {
   int64_t ldc;
   int64_t Mvalid, Nvalid;
   int64_t fp64_rows;         // mode 1: rows < fp64_rows are written as FP64 (final)
+  int c_fp64;                // mode 1: C is stored as FP64 (read and written in FP64)
   int* status;
   int64_t n_mt, n_nt, n_ks;  // work items: M tiles x N tiles x K splits
 };
@@ -654,6 +655,22 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
           // C -= product, 16 columns per batch of loads
 #pragma unroll
           for (int c16 = 0; c16 < OZ_EPI_COLS / 16; ++c16) {
+            if (a.c_fp64) {
+              // FP64 storage (a panel's own columns): one FP64 subtraction per element
+              double cd[16];
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const int64_t gn = it.n0 + part * OZ_EPI_COLS + c16 * 16 + j;
+                cd[j] = (gn < a.Nvalid) ? a.C64[gn * a.ldc + gm] : 0.0;
+              }
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const int64_t gn = it.n0 + part * OZ_EPI_COLS + c16 * 16 + j;
+                if (gn >= a.Nvalid) continue;
+                a.C64[gn * a.ldc + gm] = cd[j] - df_to_double(acc[c16 * 16 + j]);
+              }
+              continue;
+            }
             float2 cv[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
@@ -810,10 +827,11 @@ static int launch_oz(OzArgs a, unsigned gm, unsigned gn, unsigned gk, int cls, d
 
 // Trailing update in the emulated-FP64 form.  C (m x n, ld ldc) holds df64
 // pairs; rows < fp64_rows of C are written back as FP64 (finished R rows).
+// With c_fp64, C is FP64 storage instead (read and written as FP64).
 // Y: unit-lower m x nb (read from a Y\R buffer, FP64), T: nb x nb upper.
 int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
                    double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
-                   cudaStream_t s) {
+                   cudaStream_t s, bool c_fp64) {
   if (m <= 0 || n <= 0) return CANDMC_OK;
   if (nb > OZ_M) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
   const int64_t KG = 128;                       // K rows per exact accumulation
@@ -829,7 +847,8 @@ int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, M
   auto* yas = static_cast<__nv_bfloat16*>(ya.p);
   auto* cbs = static_cast<__nv_bfloat16*>(cb.p);
   CANDMC_RET(launch_slice_kcol(ysrc, 0, m, nb, AR1, Kp1, (int)KG, yas, static_cast<int*>(ea.p), s));
-  SliceSrc csrc{nullptr, reinterpret_cast<const float2*>(C), ldc, kDense, 0};
+  SliceSrc csrc = c_fp64 ? SliceSrc{C, nullptr, ldc, kDense, 0}
+                         : SliceSrc{nullptr, reinterpret_cast<const float2*>(C), ldc, kDense, 0};
   CANDMC_RET(launch_slice_kcol(csrc, 0, m, n, BR1, Kp1, (int)KG, cbs, static_cast<int*>(eb.p), s));
   // K split: about two waves of CTAs
   const int64_t ntiles = BR1 / OZ_N;
@@ -875,6 +894,7 @@ int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, M
   g2.eA = static_cast<int*>(ey2.p); g2.eB = static_cast<int*>(ez2.p);
   g2.mode = 1; g2.C = reinterpret_cast<float2*>(C); g2.C64 = C; g2.ldc = ldc;
   g2.Mvalid = m; g2.Nvalid = n; g2.fp64_rows = fp64_rows; g2.status = status;
+  g2.c_fp64 = c_fp64 ? 1 : 0;
   CANDMC_RET(launch_oz(g2, (unsigned)(AR2 / OZ_M), (unsigned)(BR2 / OZ_N), 1, CANDMC_KCLASS_OZ_NN,
                        2.0 * m * n * nb, s));
   return CANDMC_OK;

@@ -280,7 +280,10 @@ int candmc_batched_status(void* stream, int* status);
  * column; 0: level by level); "oz_reserve_sms" (SMs kept free of the
  * persistent emulated-FP64 update kernel during QR_2D_pipe, for the panel
  * stream; default 32); "pipe_leaf_rows" (leaf height of the panels QR_2D_pipe
- * factors, 32..256, default 128) */
+ * factors, 32..256, default 128); "panel_oz_min_rows" (in the emulated-FP64
+ * form, panels with at least this many rows apply each half's Q^T to the other
+ * half of the panel on the tensor cores instead of the FP64 pipe; default
+ * 2048, 0 disables) */
 int candmc_set_tuning(const char* key, int64_t value);
 
 /* ---- least-squares request server (no counterpart in the reference) ---------

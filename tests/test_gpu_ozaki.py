@@ -127,3 +127,33 @@ def test_QR_2D_ozaki_host_entry(cm):
     cm.QR_2D(Ah, 128, precision="ozaki")
     assert np.abs(Ah - Ao).max() <= 1e-10 * np.abs(Ao).max()
     assert co.backward_error(A, Ah) <= BWD_TOL
+
+
+@pytest.mark.parametrize("m,k,b,min_rows", [(1024, 512, 128, 256), (2500, 384, 128, 1024), (640, 640, 64, 1)])
+def test_panel_split_update_on_tensor_cores(cm, m, k, b, min_rows):
+    """In the emulated form, a panel's own column-half update (Q1^T on the
+    right half inside the recursive split) runs on the tensor cores with the
+    panel in FP64 storage once the panel has min_rows rows: same factorization
+    as the oracle, same backward-error bound."""
+    A = fx.gaussian(m, k, 3 * m + k + min_rows)
+    Ao = A.copy()
+    co.QR_2D(Ao, b)
+    try:
+        cm.set_tuning("panel_oz_min_rows", min_rows)
+        for entry in (cm.QR_2D, cm.QR_2D_pipe):
+            dA = dev(A)
+            entry(dA, b, precision="ozaki")
+            torch.cuda.synchronize()
+            YR = host(dA)
+            D = np.abs(YR - Ao)
+            if m == k:
+                D[-1, -1] = abs(abs(YR[-1, -1]) - abs(Ao[-1, -1]))
+            assert D.max() <= 1e-10 * np.abs(Ao).max(), D.max()
+            assert co.backward_error(A, YR) <= BWD_TOL
+    finally:
+        cm.set_tuning("panel_oz_min_rows", 2048)
+
+
+def test_panel_split_update_knob_rejects_negative(cm):
+    with pytest.raises(Exception):
+        cm.set_tuning("panel_oz_min_rows", -1)
