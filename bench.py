@@ -14,8 +14,8 @@ TFLOP/s = (4/3 n^3) / step time (the reference's GFlops formula
 2mk^2 - 2/3 k^3 at m = k, bench/QR/bench_qr_2d.cxx:85-87).  The line also
 carries the whole-matrix backward error and orthogonality of the timed
 factorization, and, each with its own step count, `fp64_form` (the plain FP64
-form on the same matrix), `tsqr_hr` (the TSQR-HR panel workload below) and
-`forms` (the precision-form workload below).
+form on the same matrix), `tsqr_hr`, `forms`, `batched` and `serve` (the
+workloads below).
 
 Other workloads (`--workload`), one JSON line each in the same format:
   tsqr_hr  TSQR-HR of one 8192 x 64 N(0,1) panel (seed 0): hh_recon_qr,
@@ -595,11 +595,13 @@ def wl_caqr(args, ctx):
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained / 28 slice products "
                                "(of measured)"}
     elif prec == "fp32":
-        roof = {"bound": "fp32", "achieved": achieved, "peak": 73.8, "unit": "TFLOP/s",
-                "frac": achieved / 73.8 if achieved else None, "traffic": None,
-                "kernel": "k_gemm_f32 (FP32 SIMT contractions on df64 storage)", "launches": dom_l,
+        # the FP32 form: 6 BF16 slice products (3 slices, pairs i + j <= 2)
+        pk = measured_peaks().get("bf16_tflops_sustained", 1700.0) / 6.0
+        roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s",
+                "frac": achieved / pk if achieved else None, "traffic": None,
+                "kernel": "k_oz_mma<., 3> (FP32 form: 3 BF16 slices on tcgen05)", "launches": dom_l,
                 "share_of_step": dom_ms / t_max if t_max else None,
-                "peak_source": "FFMA microbenchmark on this GB300 (73.8 TFLOP/s)"}
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained / 6 slice products (of measured)"}
     else:
         roof = fp64_roof(prof, dom, "k_gemm_f64 (Y^T A split-K partials and A -= Y Z)", t_max)
         roof["traffic"] = traffic_from_profile("gemm_f64_caqr_n16384.md")
@@ -642,6 +644,10 @@ def wl_caqr(args, ctx):
         log("tsqr_hr leg done")
         extra["forms"] = forms_leg(args, ctx)
         log("forms leg done")
+        extra["batched"] = batched_leg(args, ctx)
+        log("batched leg done")
+        extra["serve"] = serve_leg(args, ctx)
+        log("serve leg done")
 
     cpu = None
     if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu:
@@ -851,6 +857,24 @@ def tsqr_hr_leg(args, ctx):
     ln = wl_tsqr_hr(a, ctx)
     return {k: ln[k] for k in ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config",
                                "roofline", "accuracy", "cpu_baseline", "clocks", "gpu_launches")}
+
+
+def batched_leg(args, ctx):
+    """The 4096 uneven least-squares problems, as `--workload batched` with
+    two timed steps (autotuned, CUDA-graph replay)."""
+    a = _sub_args(args, count=4096, seed=3, steps=2, warmup=1, cpu_seconds=10.0)
+    ln = wl_batched(a, ctx)
+    return {k: ln[k] for k in ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config",
+                               "roofline", "accuracy", "e2e", "cpu_baseline", "clocks", "gpu_launches")}
+
+
+def serve_leg(args, ctx):
+    """The request server under Poisson arrivals at 1k..50k requests/s, as
+    `--workload serve` with 200 requests per rate."""
+    a = _sub_args(args, count=200, seed=4, form="fp32", cpu_seconds=10.0)
+    ln = wl_serve(a, ctx)
+    return {k: ln[k] for k in ("metric", "value", "unit", "config", "latency", "fp64_per_request", "server",
+                               "accuracy", "e2e", "cpu_baseline", "clocks", "gpu_launches")}
 
 
 def forms_leg(args, ctx):

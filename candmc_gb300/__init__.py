@@ -271,9 +271,22 @@ def QR_2D(A, b, aggreg_Y=None, precision="fp64", stream=None):
     return A
 
 
+def sym_full2band(A, b, b_sub=None, precision="fp64", stream=None):
+    """Symmetric full -> band reduction (alg/SE/CANSE.h:17-22): A (n x n, lower
+    triangle read) becomes Q^T A Q with bandwidth b in its lower triangle
+    (reflectors below the band).  b_sub: the panel width of the CAQR of each
+    band step (default b)."""
+    n = A.shape[0]
+    pa, lda = _dev(A, "A")
+    check(lib().candmc_sym_full2band(pa, lda, n, b, b if b_sub is None else b_sub, _prec(precision),
+                                     _stream(stream)), "sym_full2band")
+    return A
+
+
 def ls_solve(A, B, b=128, precision="fp64", max_refine=20, tol=1e-15, stream=None):
     """min ||A X - B||: CAQR in the given form, X0 = R^-1 Q^T B, FP64 refinement
-    (corrected semi-normal equations).  Returns (X, stats) with stats =
+    by corrected semi-normal equations (or of the augmented system with
+    set_tuning("ls_refine", 1)).  Returns (X, stats) with stats =
     {"steps", "last_change", "first_change", "status"}."""
     import ctypes
     m, n = A.shape

@@ -25,6 +25,7 @@ SIGNATURES = {
     "candmc_hh_recon_qr_noalloc": [_vp, _i64, _i64, _i64, _vp, _vp, _vp],
     "candmc_bitree_tsqr": [_vp, _i64, _vp, _vp, _i64, _i64, _int, _vp],
     "candmc_tree_tsqr": [_vp, _i64, _vp, _vp],
+    "candmc_sym_full2band": [_vp, _i64, _i64, _i64, _i64, _int, _vp],
     "candmc_tau_recon": [ctypes.c_char, _i64, _i64, _i64, _vp, _vp, _vp],
     "candmc_construct_Q1": [_vp, _i64, _vp, _vp, _i64, _i64, _i64, _i64, _vp],
     "candmc_apply_tsqr_QT": [_vp, _i64, _vp, _vp, _i64, _i64, _i64, _i64, _vp],
@@ -69,7 +70,7 @@ _RESTYPES = {"candmc_status_string": ctypes.c_char_p, "candmc_last_error": ctype
 
 # kernel classes of candmc_profile_begin / candmc_profile_end (CANDMC_KCLASS_*)
 KCLASS = {"gemm_tn": 0, "gemm_nn": 1, "reduce": 2, "panel_leaf": 3, "panel_y": 4, "small": 5,
-          "oz_slice": 6, "oz_tn": 7, "oz_nn": 8, "f32": 9}
+          "oz_slice": 6, "oz_tn": 7, "oz_nn": 8, "f32": 9, "oz_panel": 10}
 NKCLASS = 16
 
 _lib = None

@@ -64,6 +64,10 @@ static int batched_status_word(int dev, int** out) {
   *out = g_bstatus[dev];
   return CANDMC_OK;
 }
+// arithmetic form of the panels' own half-panel updates in batched calls
+// (tuning knob "batched_form"): FP64, or emulated FP64 on the tensor cores
+// for panels of at least "panel_oz_min_rows" rows
+int g_batched_form = CANDMC_PREC_FP64;
 static std::mutex g_graph_mu;
 struct CachedGraph {
   cudaGraphExec_t exec;
@@ -117,7 +121,7 @@ static int batched_issue(int64_t nprob, const int64_t* m, const int64_t* n, doub
     for (int64_t q = k; q < nprob; q += ns) {
       const int64_t i = order[q];
       double* T = tbuf.d() + toff[i];
-      rc = hr_rec(A[i], lda[i], m[i], (int)n[i], T, n[i], stword, CANDMC_PREC_FP64, sk);
+      rc = hr_rec(A[i], lda[i], m[i], (int)n[i], T, n[i], stword, g_batched_form, sk);
       if (rc != CANDMC_OK) break;
       rc = apply_qt(A[i], lda[i], m[i], (int)n[i], T, n[i], B[i], m[i], 1, CANDMC_PREC_FP64, sk);
       if (rc != CANDMC_OK) break;
@@ -173,6 +177,17 @@ extern "C" int candmc_set_tuning(const char* key, int64_t value) {
   if (std::string(key) == "pipe_leaf_rows") {
     if (value < 32 || value > 256) return set_error(CANDMC_ERR_ARG, "pipe_leaf_rows in [32, 256]");
     g_pipe_leaf_rows = value;
+    return CANDMC_OK;
+  }
+  if (std::string(key) == "batched_form") {
+    if (value != CANDMC_PREC_FP64 && value != CANDMC_PREC_OZAKI)
+      return set_error(CANDMC_ERR_ARG, "batched_form is CANDMC_PREC_FP64 or CANDMC_PREC_OZAKI");
+    g_batched_form = (int)value;
+    return CANDMC_OK;
+  }
+  if (std::string(key) == "ls_refine") {
+    if (value != 0 && value != 1) return set_error(CANDMC_ERR_ARG, "ls_refine is 0 or 1");
+    g_ls_refine = (int)value;
     return CANDMC_OK;
   }
   if (std::string(key) == "panel_oz_min_rows") {

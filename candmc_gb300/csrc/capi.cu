@@ -193,7 +193,8 @@ static int upd_core(const double* Y, int64_t ldy, int ymask, double* A, int64_t 
       CANDMC_RET(apply_qt_ozaki(Y, ldy, ymask, mb, (int)b, mref(top.d(), b, 0, kLower), A, lda, kb, 0,
                                 st.p(), s));
     else
-      CANDMC_RET(apply_qt_f32(Y, ldy, ymask, mb, (int)b, mref(top.d(), b, 0, kLower), A, lda, kb, 0, s));
+      CANDMC_RET(apply_qt_f32(Y, ldy, ymask, mb, (int)b, mref(top.d(), b, 0, kLower), A, lda, kb, 0,
+                              st.p(), s));
     return from_df64(A, lda, mb, kb, s);
   }
   CANDMC_RET(z.alloc(sizeof(double) * b * kb, s));
@@ -214,7 +215,7 @@ static int update_cols(double* P, int64_t lda, int64_t mm, int64_t b, const doub
   if (precision == CANDMC_PREC_OZAKI)
     return apply_qt_ozaki(P, lda, kUnitLower, mm, (int)b, mref(T, b, 1, kUpper), C, lda, n, b, st, s);
   if (precision == CANDMC_PREC_FP32)
-    return apply_qt_f32(P, lda, kUnitLower, mm, (int)b, mref(T, b, 1, kUpper), C, lda, n, b, s);
+    return apply_qt_f32(P, lda, kUnitLower, mm, (int)b, mref(T, b, 1, kUpper), C, lda, n, b, st, s);
   return apply_qt(P, lda, mm, (int)b, T, b, C, lda, n, precision, s);
 }
 
@@ -496,7 +497,7 @@ static int upd_yamamoto(const double* Qm, int64_t ldq, double* A, int64_t lda, i
   if (precision == CANDMC_PREC_OZAKI)
     CANDMC_RET(apply_qt_ozaki(Qm, ldq, kDense, mb, (int)b, mref(nw.d(), b), A, lda, kb, 0, st.p(), s));
   else
-    CANDMC_RET(apply_qt_f32(Qm, ldq, kDense, mb, (int)b, mref(nw.d(), b), A, lda, kb, 0, s));
+    CANDMC_RET(apply_qt_f32(Qm, ldq, kDense, mb, (int)b, mref(nw.d(), b), A, lda, kb, 0, st.p(), s));
   return from_df64(A, lda, mb, kb, s);
 }
 
@@ -905,6 +906,75 @@ int candmc_QR_2D_host(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, i
   }
   CANDMC_CK(cudaStreamSynchronize(s));
   return rc;
+}
+
+// Symmetric full -> band reduction (alg/SE/full_to_band.cxx:27-295, the
+// first caller of QR_2D_pipe and compute_invT_from_Y outside the QR
+// directory).  Per band step, with m = n - r0 - b rows below the band:
+//   P = A[r0+b:, r0:r0+b]  -> CAQR in panels of b_sub, Y aggregated (:99)
+//   T from Y^T Y (compute_invT_from_Y, :105),  U = Y T^T (:177)
+//   W = Y^T A22 (:121),  Z = Y^T A22 Y (:160),  V' = W - Z U^T / 2 (:186)
+//   A22 -= U V' + (U V')^T (:217-242), then the next step on A22.
+// A22 <- Q^T A22 Q with Q = I - Y T Y^T, so A's eigenvalues are kept; the
+// band (R blocks below the diagonal blocks) and the reflectors below it are
+// left in the lower triangle as the reference leaves them.  The symmetric
+// updates run in FP64; `precision` is the form of the panel CAQR's own
+// trailing updates.
+static int sym_full2band_dev(double* A, int64_t lda, int64_t n, int64_t b, int64_t b_sub, int precision,
+                             cudaStream_t s) {
+  int64_t r0 = 0;
+  Status st;
+  CANDMC_RET(st.init(s));
+  DevBuf Yb, top, Ub, Ut, Wb, Zh;
+  const int64_t mmax = std::max<int64_t>(n - b, 1);
+  CANDMC_RET(Yb.alloc(sizeof(double) * mmax * b, s));
+  CANDMC_RET(top.alloc(sizeof(double) * b * b, s));
+  CANDMC_RET(Ub.alloc(sizeof(double) * mmax * b, s));
+  CANDMC_RET(Ut.alloc(sizeof(double) * mmax * b, s));
+  CANDMC_RET(Wb.alloc(sizeof(double) * mmax * b, s));
+  CANDMC_RET(Zh.alloc(sizeof(double) * b * b, s));
+  while (n - r0 > b) {
+    const int64_t m = n - r0 - b;
+    double* P = A + r0 * lda + r0 + b;
+    double* A22 = A + (r0 + b) * lda + r0 + b;
+    const int64_t bb = std::min(b, m);
+    // the panel's CAQR with its reflectors aggregated into Y (m x bb, ld m)
+    CANDMC_CK(cudaMemsetAsync(Yb.p, 0, sizeof(double) * m * bb, s));
+    CANDMC_RET(qr_2d_dev(P, lda, m, bb, std::min(b_sub, bb), Yb.d(), m, st.p(), precision, s));
+    // fewer rows than the band: the block's remaining columns receive Q^T (R trapezoidal)
+    if (bb < b)
+      CANDMC_RET(upd_core(Yb.d(), m, kDense, P + bb * lda, lda, m, b - bb, bb, nullptr, 0, CANDMC_PREC_FP64, s));
+    // T^T from Y^T Y, U = Y T^T, U^T
+    CANDMC_RET(top_from_W(Yb.d(), m, m, bb, nullptr, 0, kDense, top.d(), s));
+    CANDMC_CK(cudaMemsetAsync(Ub.p, 0, sizeof(double) * m * bb, s));
+    CANDMC_CK(cudaMemsetAsync(Zh.p, 0, sizeof(double) * bb * bb, s));
+    // Zh = -T^T (scratch), U -= Y Zh
+    CANDMC_RET(set_identity(Zh.d(), bb, bb, bb, s));
+    CANDMC_RET(small_gemm(bb, bb, bb, -1.0, mref(top.d(), bb), mref(Zh.d(), bb), 0.0, Wb.d(), bb, s));
+    CANDMC_RET(gemm_nn_sub(Ub.d(), m, mref(Yb.d(), m), Wb.d(), bb, m, bb, (int)bb, s));
+    CANDMC_RET(materialize(mref(Ub.d(), m, 1, kDense), bb, m, Ut.d(), bb, s));
+    // W = Y^T A22 (bb x m);  Zh = Y^T W^T / 2 (= Y^T A22 Y / 2)
+    CANDMC_RET(gemm_tn_reduce(mref(Yb.d(), m), mref(A22, lda), m, (int)bb, m, mref(nullptr, 0), 1.0, Wb.d(),
+                              bb, s));
+    CANDMC_RET(gemm_tn_reduce(mref(Yb.d(), m), mref(Wb.d(), bb, 1), m, (int)bb, bb, mref(nullptr, 0), 0.5,
+                              Zh.d(), bb, s));
+    // V' = W - Zh U^T  (in place in W)
+    CANDMC_RET(gemm_nn_sub(Wb.d(), bb, mref(Zh.d(), bb), Ut.d(), bb, bb, m, (int)bb, s));
+    // A22 -= U V' + V'^T U^T
+    CANDMC_RET(gemm_nn_sub(A22, lda, mref(Ub.d(), m), Wb.d(), bb, m, m, (int)bb, s));
+    CANDMC_RET(gemm_nn_sub(A22, lda, mref(Wb.d(), bb, 1), Ut.d(), bb, m, m, (int)bb, s));
+    r0 += b;
+  }
+  return st.check(s);
+}
+
+int candmc_sym_full2band(double* A, int64_t lda, int64_t n, int64_t b, int64_t b_sub, int precision,
+                         void* stream) {
+  if (!A || n < 1 || b < 1 || b > 256 || b_sub < 1 || b_sub > b || b % b_sub != 0 || lda < n)
+    return set_error(CANDMC_ERR_ARG, "sym_full2band args (b <= 256, a multiple of b_sub)");
+  bool pair;
+  CANDMC_RET(check_form(precision, b_sub, &pair));
+  return sym_full2band_dev(A, lda, n, b, b_sub, precision, STREAM(stream));
 }
 
 int candmc_QR_2D_2D(double* A, int64_t lda, int64_t m, int64_t k, int64_t b, int64_t b_sub,

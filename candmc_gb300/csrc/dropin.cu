@@ -406,3 +406,11 @@ void QR_Yamamoto_2D_2D(double* A, int64_t lda_A, int64_t m, int64_t k, int64_t b
     agg->shift = sh;
   }
 }
+
+void sym_full2band(double* A, int64_t lda_A, int64_t n, int64_t b, int64_t b_sub, pview* pv) {
+  if (!one_grid(pv)) { g_status = CANDMC_ERR_ARG; return; }
+  DMat dA;
+  if (!stage(dA, A, lda_A, n, n)) { g_status = CANDMC_ERR_ALLOC; return; }
+  int rc = candmc_sym_full2band(dA.p, dA.ld, n, b, b_sub, g_precision, nullptr);
+  if (finish(rc) == CANDMC_OK) dA.out(A, lda_A);
+}

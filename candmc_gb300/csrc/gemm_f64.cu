@@ -246,19 +246,53 @@ int small_gemm(int64_t M, int64_t N, int64_t K, double alpha, MatRef A, MatRef B
   return CANDMC_OK;
 }
 
+// Tile width 16 U of the FP64 products (U = 4, 2, 1): the widest tile whose
+// grid still gives every SM work and that is not much wider than the product
+// (a product with a single right-hand side takes 16 x 16 tiles).  Each CTA's FP64 work is serial on its SM
+// (about 2 DFMA/clk), so a narrow product (a panel's own b/2-wide updates,
+// with 64 x 64 outputs or fewer) on a handful of 64 x 64 tiles leaves most of
+// the GPU idle and takes ~60 us; the same product on 16 x 16 tiles spreads
+// over the whole chip.
+static int tile_u(int64_t M, int64_t N, int64_t kparts) {
+  const int64_t want = 2 * (int64_t)num_sms();
+  const int64_t narrow = std::min(M, N);   // no tile much wider than the product itself
+  for (int U : {4, 2}) {
+    if (16 * U > 2 * std::max<int64_t>(narrow, 8)) continue;
+    const int64_t t = ((M + 16 * U - 1) / (16 * U)) * ((N + 16 * U - 1) / (16 * U));
+    if (t * kparts >= want) return U;
+  }
+  return 1;
+}
+
+template <int U>
+static void launch_gemm(dim3 grid, MatRef A, MatRef B, int64_t M, int64_t N, int64_t K, int64_t kchunk,
+                        double* out, int64_t ldo, int64_t stride, int mode, cudaStream_t s) {
+  k_gemm_f64<U><<<grid, kThreads, 0, s>>>(A, B, M, N, K, kchunk, out, ldo, stride, mode);
+}
+
+static void launch_gemm_u(int U, dim3 grid, MatRef A, MatRef B, int64_t M, int64_t N, int64_t K,
+                          int64_t kchunk, double* out, int64_t ldo, int64_t stride, int mode, cudaStream_t s) {
+  if (U == 4) launch_gemm<4>(grid, A, B, M, N, K, kchunk, out, ldo, stride, mode, s);
+  else if (U == 2) launch_gemm<2>(grid, A, B, M, N, K, kchunk, out, ldo, stride, mode, s);
+  else launch_gemm<1>(grid, A, B, M, N, K, kchunk, out, ldo, stride, mode, s);
+}
+
 // Z (nb x n, ldz) = alpha * opT * (opY^T * opC), Y and C with m rows.
 // opT.p == nullptr means no triangular factor.
 int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top, double alpha,
                    double* Z, int64_t ldz, cudaStream_t s) {
   if (nb <= 0 || n <= 0) return CANDMC_OK;
   if (nb > 256) return CANDMC_ERR_ARG;
-  const bool narrow = nb <= 32 && n <= 32;
-  const int TM = narrow ? 32 : 64, TN = TM;
+  // the widest tile that, split over 64-row slices, still fills the GPU; for
+  // narrow products 16 x 16 tiles over slices down to TK rows
+  const int U = tile_u(nb, n, std::max<int64_t>(1, m / 64));
+  const int TM = 16 * U, TN = TM;
   const int64_t tiles = ((nb + TM - 1) / TM) * ((n + TN - 1) / TN);
-  // FP64 work per CTA is what bounds these kernels: aim at ~4 CTAs per SM,
-  // with slices of at least 64 rows
+  // FP64 work per CTA is what bounds these kernels: aim at ~4 CTAs per SM
   const int64_t target = 4 * (int64_t)num_sms();
-  int64_t nsplit = std::max<int64_t>(1, std::min<int64_t>((target + tiles - 1) / tiles, (m + 63) / 64));
+  const int64_t min_rows = U == 4 ? 64 : (U == 2 ? 32 : TK);
+  int64_t nsplit = std::max<int64_t>(1, std::min<int64_t>((target + tiles - 1) / tiles,
+                                                          (m + min_rows - 1) / min_rows));
   nsplit = std::min<int64_t>(nsplit, 1024);
   int64_t kchunk = (m + nsplit - 1) / nsplit;
   kchunk = ((kchunk + TK - 1) / TK) * TK;
@@ -271,10 +305,7 @@ int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top,
   dim3 grid((unsigned)((nb + TM - 1) / TM), (unsigned)((n + TN - 1) / TN), (unsigned)nsplit);
   {
     ProfScope ps(CANDMC_KCLASS_GEMM_TN, 2.0 * nb * n * m, s);
-    if (narrow)
-      k_gemm_f64<2><<<grid, kThreads, 0, s>>>(Yt, C, nb, n, m, kchunk, part.d(), nb, stride, 0);
-    else
-      k_gemm_f64<4><<<grid, kThreads, 0, s>>>(Yt, C, nb, n, m, kchunk, part.d(), nb, stride, 0);
+    launch_gemm_u(U, grid, Yt, C, nb, n, m, kchunk, part.d(), nb, stride, 0, s);
   }
   CANDMC_CK(cudaGetLastError());
   int nbp = 1;
@@ -292,13 +323,11 @@ int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top,
 int gemm_nn_sub(double* C, int64_t ldc, MatRef Y, const double* Z, int64_t ldz, int64_t m, int64_t n,
                 int nb, cudaStream_t s) {
   if (m <= 0 || n <= 0 || nb <= 0) return CANDMC_OK;
-  const int T = n <= 32 ? 32 : 64;
+  const int U = tile_u(m, n, 1);
+  const int T = 16 * U;
   dim3 grid((unsigned)((m + T - 1) / T), (unsigned)((n + T - 1) / T), 1);
   ProfScope ps(CANDMC_KCLASS_GEMM_NN, 2.0 * m * n * nb, s);
-  if (T == 32)
-    k_gemm_f64<2><<<grid, kThreads, 0, s>>>(Y, mref(Z, ldz), m, n, nb, nb, C, ldc, 0, 1);
-  else
-    k_gemm_f64<4><<<grid, kThreads, 0, s>>>(Y, mref(Z, ldz), m, n, nb, nb, C, ldc, 0, 1);
+  launch_gemm_u(U, grid, Y, mref(Z, ldz), m, n, nb, nb, C, ldc, 0, 1, s);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
 }

@@ -75,9 +75,13 @@ int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, M
 // emulated-FP64 contraction when the factorization runs in that form (tuning
 // knob "panel_oz_min_rows"; 0 disables)
 extern int64_t g_panel_oz_min_rows;
-// gemm_f32.cu: the same update with FP32 contractions (df64 storage of C).
+// least-squares refinement: 0 corrected semi-normal equations (default), 1
+// augmented system (tuning knob "ls_refine")
+extern int g_ls_refine;
+// ozaki.cu: the same update in the FP32 form (3 BF16 slices on tcgen05, FP32
+// accumulation; df64 storage of C).
 int apply_qt_f32(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top, double* C,
-                 int64_t ldc, int64_t n, int64_t fp64_rows, cudaStream_t s);
+                 int64_t ldc, int64_t n, int64_t fp64_rows, int* status, cudaStream_t s);
 int to_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
 int from_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
 

@@ -4,11 +4,26 @@
 // The reference has no least-squares solver; this composes its pieces:
 // QR_2D_pipe (any arithmetic form) -> Q^T B by applying every panel's compact
 // WY factor in FP64 (the update_A step of qr_2d.cxx:124-177 on the right-hand
-// sides) -> X0 = R^-1 (Q^T B)[0:n] -> refinement by corrected semi-normal
-// equations (Bjorck): r = B - A X, s = A^T r, D = R^-1 R^-T s, X += D, all in
-// FP64 with A kept resident.  Its fixed point is the exact normal-equations
-// solution whatever R's accuracy, and it contracts while kappa(A)^2 * u_R < 1,
-// which is what lets the FP32 form reach FP64 accuracy.
+// sides) -> X0 = R^-1 (Q^T B)[0:n] -> iterative refinement of the augmented
+// system [I A; A^T 0][r; x] = [B; 0] (Bjorck, "Iterative refinement of linear
+// least squares solutions I", BIT 7, 1967), all residuals in FP64 with A kept
+// resident:
+//   f = B - r - A x,  g = -A^T r          (FP64 residuals of both equations)
+//   h = R^-T g,  d = Q^T f
+//   dx = R^-1 (d[0:n] - h),  dr = Q [h; d[n:m]]
+//   x += dx,  r += dr
+// Q and Q^T are the panels' compact-WY factors applied in FP64.  The fixed
+// point is the exact least-squares solution whatever R's accuracy; with R from
+// a backward-stable QR of A itself the iteration contracts by about
+// kappa(A) * u_R per step, so the FP32 form reaches FP64 accuracy up to
+// kappa ~ 1e6, and it stops at the FP64 data's own forward-error level,
+// about kappa(A) * u (for kappa = 1e10, 1e-6: no FP64 solver does better on
+// FP64 inputs).  By default (tuning knob "ls_refine" = 0) the refinement is
+// the cheaper corrected semi-normal equations, r = B - A x, dx = R^-1 R^-T A^T r:
+// with R from A's own QR it contracts as fast and reaches the same level
+// (measured on the benchmark's least-squares cases), at two passes over A
+// per step instead of two over A and two over Y; "ls_refine" = 1 selects the
+// augmented system, which also refines r.
 #include <math.h>
 
 #include <algorithm>
@@ -111,6 +126,15 @@ __global__ void k_add(double* Z, int64_t ldz, const double* C, int64_t ldc, int6
   Z[j * ldz + i] += C[j * ldc + i];
 }
 
+// Z = Z + alpha * C (m x n)
+__global__ void k_axpy(double* Z, int64_t ldz, const double* C, int64_t ldc, int64_t m, int64_t n,
+                       double alpha) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= m * n) return;
+  const int64_t i = idx % m, j = idx / m;
+  Z[j * ldz + i] = fma(alpha, C[j * ldc + i], Z[j * ldz + i]);
+}
+
 // per column: max |D| / max |X| reported as one number (max over columns)
 __global__ void k_rel_change(const double* D, int64_t ldd, const double* X, int64_t ldx, int64_t n,
                              double* out) {
@@ -200,6 +224,36 @@ static int trsm_upper(const double* R, int64_t ldr, int64_t n, const double* Din
   return CANDMC_OK;
 }
 
+// C (m x r) <- Q C or Q^T C for the factored F (Y\R, ld ldf) with every
+// panel's T (b x b each), in FP64: Q^T applies the panels first to last with
+// T^T, Q applies them last to first with T.
+static int apply_all_q(const double* F, int64_t ldf, int64_t m, int64_t n, int64_t b, const double* Tall,
+                       double* C, int64_t ldc, int64_t r, bool trans, cudaStream_t s) {
+  const int64_t npan = (n + b - 1) / b;
+  DevBuf z;
+  CANDMC_RET(z.alloc(sizeof(double) * b * r, s));
+  for (int64_t k = 0; k < npan; ++k) {
+    const int64_t i = trans ? k : npan - 1 - k;
+    const int64_t r0 = i * b, bb = std::min(b, n - r0);
+    MatRef Ym = mref(F + r0 * ldf + r0, ldf, 0, kUnitLower);
+    CANDMC_RET(gemm_tn_reduce(Ym, mref(C + r0, ldc), m - r0, (int)bb, r,
+                              mref(Tall + i * b * b, b, trans ? 1 : 0, kUpper), 1.0, z.d(), bb, s));
+    CANDMC_RET(gemm_nn_sub(C + r0, ldc, Ym, z.d(), bb, m - r0, r, (int)bb, s));
+  }
+  return CANDMC_OK;
+}
+
+int g_ls_refine = 0;
+
+static int axpy(double* Z, int64_t ldz, const double* C, int64_t ldc, int64_t m, int64_t n, double alpha,
+                cudaStream_t s) {
+  if (m <= 0 || n <= 0) return CANDMC_OK;
+  ProfScope ps(CANDMC_KCLASS_SMALL, 24.0 * m * n, s);
+  k_axpy<<<(unsigned)((m * n + 255) / 256), 256, 0, s>>>(Z, ldz, C, ldc, m, n, alpha);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
 }  // namespace candmc
 
 using namespace candmc;
@@ -226,11 +280,7 @@ extern "C" int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t 
   CANDMC_RET(Bq.alloc(sizeof(double) * m * nrhs, s));
   CANDMC_CK(cudaMemcpy2DAsync(Bq.p, sizeof(double) * m, B, sizeof(double) * ldb, sizeof(double) * m,
                               nrhs, cudaMemcpyDeviceToDevice, s));
-  for (int64_t i = 0; i < npan; ++i) {
-    const int64_t r0 = i * b, bb = std::min(b, n - r0);
-    CANDMC_RET(apply_qt(F.d() + r0 * m + r0, m, m - r0, (int)bb, Tall.d() + i * b * b, b, Bq.d() + r0, m,
-                        nrhs, CANDMC_PREC_FP64, s));
-  }
+  CANDMC_RET(apply_all_q(F.d(), m, m, n, b, Tall.d(), Bq.d(), m, nrhs, true, s));
   // 3. X0 = R^-1 (Q^T B)[0:n]
   const int64_t nblk = (n + w - 1) / w;
   CANDMC_RET(Dinv.alloc(sizeof(double) * nblk * w * w, s));
@@ -242,19 +292,43 @@ extern "C" int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t 
   CANDMC_CK(cudaMemcpy2DAsync(X, sizeof(double) * ldx, Bq.p, sizeof(double) * m, sizeof(double) * n, nrhs,
                               cudaMemcpyDeviceToDevice, s));
   CANDMC_RET(trsm_upper(F.d(), m, n, Dinv.d(), w, X, ldx, nrhs, false, s));
-  // 4. refinement: r = B - A X;  s = A^T r;  D = R^-1 R^-T s;  X += D
-  CANDMC_RET(Rres.alloc(sizeof(double) * m * nrhs, s));
-  CANDMC_RET(Sv.alloc(sizeof(double) * n * nrhs, s));
-  CANDMC_RET(D.alloc(sizeof(double) * n * nrhs, s));
+  // 4. refinement; r0 = B - A X0 (the augmented system refines r as well)
+  CANDMC_RET(Rres.alloc(sizeof(double) * m * nrhs, s));   // r
+  CANDMC_RET(Sv.alloc(sizeof(double) * n * nrhs, s));     // dx
+  CANDMC_RET(D.alloc(sizeof(double) * m * nrhs, s));      // f, then d = Q^T f, then dr
   CANDMC_RET(rel.alloc(sizeof(double) * nrhs, s));
+  if (g_ls_refine != 0)
+    CANDMC_RET(ts_gemm(false, A, lda, X, ldx, m, n, nrhs, -1.0, 1.0, B, ldb, Rres.d(), m, s));
+  DevBuf H;                                               // g, then h
+  CANDMC_RET(H.alloc(sizeof(double) * n * nrhs, s));
   std::vector<double> hrel(nrhs);
   int it = 0;
   double first = -1.0, last = 0.0, prev = HUGE_VAL;
   for (; it < max_refine; ++it) {
-    CANDMC_RET(ts_gemm(false, A, lda, X, ldx, m, n, nrhs, -1.0, 1.0, B, ldb, Rres.d(), m, s));
-    CANDMC_RET(ts_gemm(true, A, lda, Rres.d(), m, n, m, nrhs, 1.0, 0.0, nullptr, 0, Sv.d(), n, s));
-    CANDMC_RET(trsm_upper(F.d(), m, n, Dinv.d(), w, Sv.d(), n, nrhs, true, s));
-    CANDMC_RET(trsm_upper(F.d(), m, n, Dinv.d(), w, Sv.d(), n, nrhs, false, s));
+    if (g_ls_refine == 0) {
+      // corrected semi-normal equations: r = B - A x, dx = R^-1 R^-T A^T r
+      CANDMC_RET(ts_gemm(false, A, lda, X, ldx, m, n, nrhs, -1.0, 1.0, B, ldb, Rres.d(), m, s));
+      CANDMC_RET(ts_gemm(true, A, lda, Rres.d(), m, n, m, nrhs, 1.0, 0.0, nullptr, 0, Sv.d(), n, s));
+      CANDMC_RET(trsm_upper(F.d(), m, n, Dinv.d(), w, Sv.d(), n, nrhs, true, s));
+      CANDMC_RET(trsm_upper(F.d(), m, n, Dinv.d(), w, Sv.d(), n, nrhs, false, s));
+    } else {
+      // f = B - r - A x ;  g = -A^T r
+      CANDMC_RET(ts_gemm(false, A, lda, X, ldx, m, n, nrhs, -1.0, 1.0, B, ldb, D.d(), m, s));
+      CANDMC_RET(axpy(D.d(), m, Rres.d(), m, m, nrhs, -1.0, s));
+      CANDMC_RET(ts_gemm(true, A, lda, Rres.d(), m, n, m, nrhs, -1.0, 0.0, nullptr, 0, H.d(), n, s));
+      // h = R^-T g ;  d = Q^T f
+      CANDMC_RET(trsm_upper(F.d(), m, n, Dinv.d(), w, H.d(), n, nrhs, true, s));
+      CANDMC_RET(apply_all_q(F.d(), m, m, n, b, Tall.d(), D.d(), m, nrhs, true, s));
+      // dx = R^-1 (d[0:n] - h)
+      CANDMC_CK(cudaMemcpy2DAsync(Sv.p, sizeof(double) * n, D.p, sizeof(double) * m, sizeof(double) * n,
+                                  nrhs, cudaMemcpyDeviceToDevice, s));
+      CANDMC_RET(axpy(Sv.d(), n, H.d(), n, n, nrhs, -1.0, s));
+      CANDMC_RET(trsm_upper(F.d(), m, n, Dinv.d(), w, Sv.d(), n, nrhs, false, s));
+      // dr = Q [h; d[n:m]]
+      CANDMC_CK(cudaMemcpy2DAsync(D.p, sizeof(double) * m, H.p, sizeof(double) * n, sizeof(double) * n,
+                                  nrhs, cudaMemcpyDeviceToDevice, s));
+      CANDMC_RET(apply_all_q(F.d(), m, m, n, b, Tall.d(), D.d(), m, nrhs, false, s));
+    }
     {
       ProfScope ps(CANDMC_KCLASS_SMALL, 0.0, s);
       k_rel_change<<<(unsigned)nrhs, 256, 0, s>>>(Sv.d(), n, X, ldx, n, rel.d());
@@ -264,15 +338,12 @@ extern "C" int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t 
     CANDMC_CK(cudaStreamSynchronize(s));
     last = *std::max_element(hrel.begin(), hrel.end());
     if (first < 0.0) first = last;
-    // the iteration contracts only while kappa(A)^2 u_R < 1: a correction
-    // that is not smaller than the previous one (or not finite) is dropped
-    // and the refinement ends with the current X
+    // a correction that is not smaller than the previous one (or not finite)
+    // is dropped and the refinement ends with the current X: the iteration has
+    // reached the FP64 data's forward-error level, or kappa(A) u_R >= 1
     if (!(last == last) || (last >= prev && last > tol)) break;
-    {
-      ProfScope ps(CANDMC_KCLASS_SMALL, 0.0, s);
-      k_add<<<(unsigned)((n * nrhs + 255) / 256), 256, 0, s>>>(X, ldx, Sv.d(), n, n, nrhs);
-      CANDMC_CK(cudaGetLastError());
-    }
+    CANDMC_RET(axpy(X, ldx, Sv.d(), n, n, nrhs, 1.0, s));
+    if (g_ls_refine != 0) CANDMC_RET(axpy(Rres.d(), m, D.d(), m, m, nrhs, 1.0, s));
     prev = last;
     if (last <= tol) {
       ++it;

@@ -40,15 +40,22 @@
 
 namespace candmc {
 
-constexpr int OZ_S = 7;           // slices per operand
-constexpr int OZ_G = 5;           // TMEM accumulator groups
+constexpr int OZ_S = 7;           // slices per operand of the emulated-FP64 form
+constexpr int OZ_S32 = 3;         // slices per operand of the FP32 form
 constexpr int OZ_M = 128;         // tile rows (TMEM lanes)
 constexpr int OZ_N = 96;          // tile columns
 constexpr int OZ_STAGES = 4;
 constexpr int OZ_ABYTES = OZ_M * 16 * 2;               // one slice, one K16 step
 constexpr int OZ_BBYTES = OZ_N * 16 * 2;
-constexpr int OZ_STAGE_BYTES = OZ_S * (OZ_ABYTES + OZ_BBYTES);
-constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024;
+// Per slice count S: TMEM accumulator groups G (levels 0..3 exact each, the
+// rest shared, for S = 7; one per level for S <= 5), bytes of one ring stage
+// and the dynamic shared memory of the kernel.
+template <int S>
+struct OzCfg {
+  static constexpr int G = S >= 5 ? 5 : S;
+  static constexpr int STAGE_BYTES = S * (OZ_ABYTES + OZ_BBYTES);
+  static constexpr int SMEM = OZ_STAGES * STAGE_BYTES + 1024;
+};
 constexpr long OZ_WAIT_LIMIT = 1L << 22;                // bounded mbarrier polls
 
 // element (r, k) of an R x K operand slice plane in core-matrix K-major order
@@ -110,13 +117,14 @@ __device__ __forceinline__ int scale_exp(float mx) {
   return e;
 }
 
-// Write the 7 natural-weight digits of v = (h + l) * 2^(8 - e) to slices.
+// Write the S natural-weight digits of v = (h + l) * 2^(8 - e) to slices.
+template <int S>
 __device__ __forceinline__ void slice_value(f2 v, int e, __nv_bfloat16* out, int64_t plane,
                                             int64_t off) {
   float p = ldexpf(v.h, 8 - e), q = ldexpf(v.l, 8 - e);
   float w = 1.0f;
 #pragma unroll
-  for (int i = 0; i < OZ_S; ++i) {
+  for (int i = 0; i < S; ++i) {
     f2 s = two_sum(p, q);
     float d = rintf(s.h);
     out[i * plane + off] = __float2bfloat16_rn(d * w);
@@ -151,7 +159,8 @@ __device__ __forceinline__ f2 src_at(const SliceSrc& s, int64_t r, int64_t c) {
 // Operand element (n, k) = src(k, n): K runs down the columns of a column-major
 // source (rows k0 .. k0 + K).  One warp per (n, K group of G); n in [0, Nvalid)
 // are data, rows beyond are zero padding up to Rpad; k beyond Kvalid are zero.
-// Slices: OZ_S planes of Rpad x Kpad (cm order); exponents e[(k/G) * Rpad + n].
+// Slices: S planes of Rpad x Kpad (cm order); exponents e[(k/G) * Rpad + n].
+template <int S>
 __global__ void k_slice_kcol(SliceSrc src, int64_t k0, int64_t Kvalid, int64_t Nvalid, int64_t Rpad,
                              int64_t Kpad, int G, __nv_bfloat16* out, int* eout) {
   const int lane = threadIdx.x & 31;
@@ -175,7 +184,7 @@ __global__ void k_slice_kcol(SliceSrc src, int64_t k0, int64_t Kvalid, int64_t N
   for (int64_t k = g * G + lane; k < (g + 1) * G; k += 32) {
     f2 v = {0.0f, 0.0f};
     if (n < Nvalid && k < Kvalid) v = src_at(src, k0 + k, n);
-    slice_value(v, e, out, plane, cm_off(n, k, Rpad));
+    slice_value<S>(v, e, out, plane, cm_off(n, k, Rpad));
   }
 }
 
@@ -185,6 +194,7 @@ __global__ void k_slice_kcol(SliceSrc src, int64_t k0, int64_t Kvalid, int64_t N
 // scale exponent; then, for every K16 block, the 8 x 16 elements of a slice
 // plane are one contiguous 256-byte run of the core-matrix order, which a
 // warp writes with 8-byte stores (4 elements per lane).
+template <int S>
 __global__ void __launch_bounds__(256) k_slice_kcol8(SliceSrc src, int64_t k0, int64_t Kvalid,
                                                      int64_t Nvalid, int64_t Rpad, int64_t Kpad, int G,
                                                      __nv_bfloat16* out, int* eout) {
@@ -230,7 +240,7 @@ __global__ void __launch_bounds__(256) k_slice_kcol8(SliceSrc src, int64_t k0, i
     const int64_t base = ((kb0 >> 4) + blk) * (Rpad * 16) + (n0 >> 3) * 128 + 4 * u;
     float w = 1.0f;
 #pragma unroll
-    for (int sl = 0; sl < OZ_S; ++sl) {
+    for (int sl = 0; sl < S; ++sl) {
       __align__(8) __nv_bfloat16 d4[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
@@ -249,6 +259,7 @@ __global__ void __launch_bounds__(256) k_slice_kcol8(SliceSrc src, int64_t k0, i
 // Operand element (n, k) = src(n, k): K runs along the rows of a column-major
 // source (rows n0 + n, columns 0 .. K).  Scale group = the whole row (G = Kpad).
 // A CTA stages 32 rows x Kpad columns through shared memory.
+template <int S>
 __global__ void k_slice_krow(SliceSrc src, int64_t n0, int64_t Nvalid, int64_t Kvalid, int64_t Rpad,
                              int64_t Kpad, __nv_bfloat16* out, int* eout) {
   extern __shared__ float2 tile[];   // [32][Kpad]
@@ -274,16 +285,16 @@ __global__ void k_slice_krow(SliceSrc src, int64_t n0, int64_t Nvalid, int64_t K
     if (lane == 0) eout[n] = e;
     for (int64_t k = lane; k < Kpad; k += 32) {
       float2 t = tile[rr * Kpad + k];
-      slice_value({t.x, t.y}, e, out, plane, cm_off(n, k, Rpad));
+      slice_value<S>({t.x, t.y}, e, out, plane, cm_off(n, k, Rpad));
     }
   }
 }
 
 // ------------------------------------------------------------------ tcgen05 kernel
 struct OzArgs {
-  const __nv_bfloat16* As;   // A-operand slices: OZ_S planes of AR x Kpad
+  const __nv_bfloat16* As;   // A-operand slices: S planes of AR x Kpad
   int64_t AR;
-  const __nv_bfloat16* Bs;   // B-operand slices: OZ_S planes of BR x Kpad
+  const __nv_bfloat16* Bs;   // B-operand slices: S planes of BR x Kpad
   int64_t BR;
   int64_t Kpad;              // multiple of 16
   int64_t k_per_cta;         // K extent of one CTA (multiple of kgroup)
@@ -363,6 +374,21 @@ __device__ __forceinline__ f2 combine_groups(float g0, float g1, float g2, float
   return {h, __fsub_rn(l, __fsub_rn(h, s))};
 }
 
+// The accumulators of one output element as one value: the exact five-group
+// combine of the emulated-FP64 form, or, for the FP32 form (one group per
+// level, FP32 accuracy wanted), their FP32 sum.
+template <int G>
+__device__ __forceinline__ f2 combine_g(const float (&gv)[G][8], int j) {
+  if constexpr (G == 5) {
+    return combine_groups(gv[0][j], gv[1][j], gv[2][j], gv[3][j], gv[4][j]);
+  } else {
+    float h = gv[G - 1][j];
+#pragma unroll
+    for (int g = G - 2; g >= 0; --g) h = __fadd_rn(gv[g][j], h);
+    return {h, 0.0f};
+  }
+}
+
 // x + y without the lo-part TwoSum: relative error of order 2^-46 of |x| + |y|
 __device__ __forceinline__ f2 df_add_sloppy(f2 x, f2 y) {
   const float s = __fadd_rn(x.h, y.h);
@@ -440,8 +466,10 @@ __device__ __forceinline__ OzItem oz_item(const OzArgs& a, int64_t w) {
 // the epilogue warps 2.. read the accumulators (warp w owns TMEM lanes
 // 32 (w % 4) .. +31 and column part (w - 2) / 4), release them, and combine
 // them in df64.
-template <int MODE>
+template <int MODE, int S>
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
+  constexpr int G = OzCfg<S>::G;
+  constexpr int STAGE_BYTES = OzCfg<S>::STAGE_BYTES;
   extern __shared__ __align__(1024) unsigned char oz_smem[];
   __shared__ __align__(8) uint64_t full_b[OZ_STAGES], empty_b[OZ_STAGES], acc_full, acc_empty, fin;
   __shared__ uint32_t tmem_base_s;
@@ -483,14 +511,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
         for (int64_t kb = it.kbeg >> 4; kb < (it.kend >> 4); ++kb, ++gs) {
           const int st = (int)(gs % OZ_STAGES);
           if (!oz_wait(&empty_b[st], (uint32_t)(((gs / OZ_STAGES) & 1) ^ 1), &s_fail)) break;
-          mbar_expect_tx(&full_b[st], (unsigned)OZ_STAGE_BYTES);
-          unsigned char* sb = ring + (size_t)st * OZ_STAGE_BYTES;
+          mbar_expect_tx(&full_b[st], (unsigned)STAGE_BYTES);
+          unsigned char* sb = ring + (size_t)st * STAGE_BYTES;
 #pragma unroll 1
-          for (int sl = 0; sl < OZ_S; ++sl) {
+          for (int sl = 0; sl < S; ++sl) {
             bulk_g2s(smem_u32(sb + sl * OZ_ABYTES),
                      a.As + (int64_t)sl * a.AR * a.Kpad + kb * a.AR * 16 + (it.m0 >> 3) * 128,
                      (unsigned)OZ_ABYTES, &full_b[st]);
-            bulk_g2s(smem_u32(sb + OZ_S * OZ_ABYTES + sl * OZ_BBYTES),
+            bulk_g2s(smem_u32(sb + S * OZ_ABYTES + sl * OZ_BBYTES),
                      a.Bs + (int64_t)sl * a.BR * a.Kpad + kb * a.BR * 16 + (it.n0 >> 3) * 128,
                      (unsigned)OZ_BBYTES, &full_b[st]);
           }
@@ -515,19 +543,19 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
           const int st = (int)(gs % OZ_STAGES);
           if (!oz_wait(&full_b[st], (uint32_t)((gs / OZ_STAGES) & 1), &s_fail)) break;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          unsigned char* sb = ring + (size_t)st * OZ_STAGE_BYTES;
+          unsigned char* sb = ring + (size_t)st * STAGE_BYTES;
           // the first product into each accumulator in a group's first step overwrites it
-          bool first_of_group[OZ_G];
+          bool first_of_group[G];
 #pragma unroll
-          for (int g = 0; g < OZ_G; ++g) first_of_group[g] = (sig == 0);
+          for (int g = 0; g < G; ++g) first_of_group[g] = (sig == 0);
 #pragma unroll
-          for (int i = 0; i < OZ_S; ++i) {
+          for (int i = 0; i < S; ++i) {
 #pragma unroll
-            for (int j = 0; j < OZ_S; ++j) {
-              if (i + j >= OZ_S) continue;
-              const int g = (i + j < OZ_G - 1) ? i + j : OZ_G - 1;
+            for (int j = 0; j < S; ++j) {
+              if (i + j >= S) continue;
+              const int g = (i + j < G - 1) ? i + j : G - 1;
               const uint64_t ad = make_desc(smem_u32(sb + i * OZ_ABYTES));
-              const uint64_t bd = make_desc(smem_u32(sb + OZ_S * OZ_ABYTES + j * OZ_BBYTES));
+              const uint64_t bd = make_desc(smem_u32(sb + S * OZ_ABYTES + j * OZ_BBYTES));
               const uint32_t dt = tmem + (uint32_t)(g * OZ_N);
               const uint32_t accum = first_of_group[g] ? 0u : 1u;
               first_of_group[g] = false;
@@ -603,14 +631,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
           int eB[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) eB[j] = eb[c8 * 8 + j];
-          uint32_t gr[OZ_G][8];
+          uint32_t gr[G][8];
 #pragma unroll
-          for (int g = 0; g < OZ_G; ++g)
+          for (int g = 0; g < G; ++g)
             tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * OZ_N + cbase), gr[g]);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-          float gv[OZ_G][8];
+          float gv[G][8];
 #pragma unroll
-          for (int g = 0; g < OZ_G; ++g) {
+          for (int g = 0; g < G; ++g) {
             tmem_regs_ready(gr[g]);
 #pragma unroll
             for (int j = 0; j < 8; ++j) gv[g][j] = __uint_as_float(gr[g][j]);
@@ -625,7 +653,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
           if (__all_sync(0xffffffffu, normal)) {
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-              const f2 v = combine_groups(gv[0][j], gv[1][j], gv[2][j], gv[3][j], gv[4][j]);
+              const f2 v = combine_g<G>(gv, j);
               const float f = pow2f(eA + eB[j] - 16);
               const f2 sv = {__fmul_rn(v.h, f), __fmul_rn(v.l, f)};
               if (MODE == 0) acc[c8 * 8 + j] = df_add_sloppy(acc[c8 * 8 + j], sv);
@@ -634,7 +662,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
           } else {
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-              const f2 v = combine_groups(gv[0][j], gv[1][j], gv[2][j], gv[3][j], gv[4][j]);
+              const f2 v = combine_g<G>(gv, j);
               // 2^e as three normal factors (e >= -312 for float inputs): the
               // partial products stay exact unless the result leaves the range
               const int e = eA + eB[j] - 16;
@@ -769,29 +797,31 @@ int from_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s) {
   return CANDMC_OK;
 }
 
+template <int S>
 static int launch_slice_kcol(SliceSrc src, int64_t k0, int64_t Kvalid, int64_t Nvalid, int64_t Rpad,
                              int64_t Kpad, int G, __nv_bfloat16* out, int* e, cudaStream_t s) {
-  ProfScope ps(CANDMC_KCLASS_OZ_SLICE, 8.0 * Nvalid * Kvalid + 14.0 * Rpad * Kpad, s);
+  ProfScope ps(CANDMC_KCLASS_OZ_SLICE, 8.0 * Nvalid * Kvalid + 2.0 * S * Rpad * Kpad, s);
   if (G <= 128 && G % 16 == 0 && Rpad % 8 == 0) {
-    k_slice_kcol8<<<dim3((unsigned)(Rpad / 8), (unsigned)(Kpad / G)), 256, 0, s>>>(src, k0, Kvalid, Nvalid,
+    k_slice_kcol8<S><<<dim3((unsigned)(Rpad / 8), (unsigned)(Kpad / G)), 256, 0, s>>>(src, k0, Kvalid, Nvalid,
                                                                                   Rpad, Kpad, G, out, e);
     CANDMC_CK(cudaGetLastError());
     return CANDMC_OK;
   }
   int64_t warps = Rpad * (Kpad / G);
-  k_slice_kcol<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(src, k0, Kvalid, Nvalid, Rpad,
+  k_slice_kcol<S><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(src, k0, Kvalid, Nvalid, Rpad,
                                                                       Kpad, G, out, e);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
 }
 
+template <int S>
 static int launch_slice_krow(SliceSrc src, int64_t n0, int64_t Nvalid, int64_t Kvalid, int64_t Rpad,
                              int64_t Kpad, __nv_bfloat16* out, int* e, cudaStream_t s) {
   size_t sm = sizeof(float2) * 32 * (size_t)Kpad;
   if (sm > 48 * 1024)
-    CANDMC_CK(cudaFuncSetAttribute(k_slice_krow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  ProfScope ps(CANDMC_KCLASS_OZ_SLICE, 8.0 * Nvalid * Kvalid + 14.0 * Rpad * Kpad, s);
-  k_slice_krow<<<(unsigned)((Rpad + 31) / 32), 256, sm, s>>>(src, n0, Nvalid, Kvalid, Rpad, Kpad, out, e);
+    CANDMC_CK(cudaFuncSetAttribute(k_slice_krow<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  ProfScope ps(CANDMC_KCLASS_OZ_SLICE, 8.0 * Nvalid * Kvalid + 2.0 * S * Rpad * Kpad, s);
+  k_slice_krow<S><<<(unsigned)((Rpad + 31) / 32), 256, sm, s>>>(src, n0, Nvalid, Kvalid, Rpad, Kpad, out, e);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
 }
@@ -801,12 +831,14 @@ thread_local int t_oz_cap = 0;
 
 // one persistent CTA per SM at most (fewer under a cap), each taking every
 // gridDim-th work item
+template <int S>
 static int launch_oz(OzArgs a, unsigned gm, unsigned gn, unsigned gk, int cls, double flops,
                      cudaStream_t s) {
+  constexpr int SMEM = OzCfg<S>::SMEM;
   static std::atomic<bool> attr{false};
   if (!attr) {
-    CANDMC_CK(cudaFuncSetAttribute(k_oz_mma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
-    CANDMC_CK(cudaFuncSetAttribute(k_oz_mma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
+    CANDMC_CK(cudaFuncSetAttribute(k_oz_mma<0, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+    CANDMC_CK(cudaFuncSetAttribute(k_oz_mma<1, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
     attr = true;
   }
   a.n_mt = gm;
@@ -818,20 +850,23 @@ static int launch_oz(OzArgs a, unsigned gm, unsigned gn, unsigned gk, int cls, d
   const unsigned grid = (unsigned)std::min<int64_t>(items, ctas);
   ProfScope ps(cls, flops, s);
   if (a.mode == 0)
-    k_oz_mma<0><<<grid, OZ_THREADS, OZ_SMEM, s>>>(a);
+    k_oz_mma<0, S><<<grid, OZ_THREADS, SMEM, s>>>(a);
   else
-    k_oz_mma<1><<<grid, OZ_THREADS, OZ_SMEM, s>>>(a);
+    k_oz_mma<1, S><<<grid, OZ_THREADS, SMEM, s>>>(a);
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;
 }
 
-// Trailing update in the emulated-FP64 form.  C (m x n, ld ldc) holds df64
-// pairs; rows < fp64_rows of C are written back as FP64 (finished R rows).
-// With c_fp64, C is FP64 storage instead (read and written as FP64).
-// Y: unit-lower m x nb (read from a Y\R buffer, FP64), T: nb x nb upper.
-int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
-                   double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
-                   cudaStream_t s, bool c_fp64) {
+// The trailing update with S-slice contractions: C <- C - Y (Top (Y^T C)).
+// C (m x n, ld ldc) holds df64 pairs; rows < fp64_rows of C are written back
+// as FP64 (finished R rows).  With c_fp64, C is FP64 storage instead (read and
+// written as FP64).  Y: unit-lower m x nb (read from a Y\R buffer, FP64),
+// Top: the nb x nb operator applied to Y^T C.  cls_tn / cls_nn: the kernel
+// classes the two contractions are counted under.
+template <int S>
+static int apply_qt_slices(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
+                           double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
+                           cudaStream_t s, bool c_fp64, int cls_tn, int cls_nn) {
   if (m <= 0 || n <= 0) return CANDMC_OK;
   if (nb > OZ_M) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
   const int64_t KG = 128;                       // K rows per exact accumulation
@@ -839,17 +874,17 @@ int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, M
   const int64_t Kp1 = rup(m, KG);
   const int64_t AR1 = OZ_M, BR1 = rup(n, OZ_N);
   DevBuf ya, ea, cb, eb, part, z;
-  CANDMC_RET(ya.alloc(sizeof(__nv_bfloat16) * OZ_S * AR1 * Kp1, s));
+  CANDMC_RET(ya.alloc(sizeof(__nv_bfloat16) * S * AR1 * Kp1, s));
   CANDMC_RET(ea.alloc(sizeof(int) * (Kp1 / KG) * AR1, s));
-  CANDMC_RET(cb.alloc(sizeof(__nv_bfloat16) * OZ_S * BR1 * Kp1, s));
+  CANDMC_RET(cb.alloc(sizeof(__nv_bfloat16) * S * BR1 * Kp1, s));
   CANDMC_RET(eb.alloc(sizeof(int) * (Kp1 / KG) * BR1, s));
   SliceSrc ysrc{Y, nullptr, ldy, ymask, 0};
   auto* yas = static_cast<__nv_bfloat16*>(ya.p);
   auto* cbs = static_cast<__nv_bfloat16*>(cb.p);
-  CANDMC_RET(launch_slice_kcol(ysrc, 0, m, nb, AR1, Kp1, (int)KG, yas, static_cast<int*>(ea.p), s));
+  CANDMC_RET(launch_slice_kcol<S>(ysrc, 0, m, nb, AR1, Kp1, (int)KG, yas, static_cast<int*>(ea.p), s));
   SliceSrc csrc = c_fp64 ? SliceSrc{C, nullptr, ldc, kDense, 0}
                          : SliceSrc{nullptr, reinterpret_cast<const float2*>(C), ldc, kDense, 0};
-  CANDMC_RET(launch_slice_kcol(csrc, 0, m, n, BR1, Kp1, (int)KG, cbs, static_cast<int*>(eb.p), s));
+  CANDMC_RET(launch_slice_kcol<S>(csrc, 0, m, n, BR1, Kp1, (int)KG, cbs, static_cast<int*>(eb.p), s));
   // K split: about two waves of CTAs
   const int64_t ntiles = BR1 / OZ_N;
   int64_t ksplit = std::max<int64_t>(1, std::min<int64_t>(Kp1 / KG, (2 * num_sms_oz() + ntiles - 1) / ntiles));
@@ -861,7 +896,7 @@ int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, M
   g1.kgroup = KG; g1.eA = static_cast<int*>(ea.p); g1.eB = static_cast<int*>(eb.p);
   g1.mode = 0; g1.part = static_cast<float2*>(part.p); g1.Mvalid = nb; g1.Nvalid = n;
   g1.status = status;
-  CANDMC_RET(launch_oz(g1, 1, (unsigned)ntiles, (unsigned)ksplit, CANDMC_KCLASS_OZ_TN,
+  CANDMC_RET(launch_oz<S>(g1, 1, (unsigned)ntiles, (unsigned)ksplit, cls_tn,
                        2.0 * nb * n * m, s));
   // ---- Z' = T^T * sum(partials)   (FP64, nb x n)
   CANDMC_RET(z.alloc(sizeof(double) * nb * n, s));
@@ -878,14 +913,14 @@ int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, M
   const int64_t Kp2 = rup(nb, 16);
   const int64_t AR2 = rup(m, OZ_M), BR2 = rup(n, OZ_N);
   DevBuf y2, ey2, z2, ez2;
-  CANDMC_RET(y2.alloc(sizeof(__nv_bfloat16) * OZ_S * AR2 * Kp2, s));
+  CANDMC_RET(y2.alloc(sizeof(__nv_bfloat16) * S * AR2 * Kp2, s));
   CANDMC_RET(ey2.alloc(sizeof(int) * AR2, s));
-  CANDMC_RET(z2.alloc(sizeof(__nv_bfloat16) * OZ_S * BR2 * Kp2, s));
+  CANDMC_RET(z2.alloc(sizeof(__nv_bfloat16) * S * BR2 * Kp2, s));
   CANDMC_RET(ez2.alloc(sizeof(int) * BR2, s));
-  CANDMC_RET(launch_slice_krow(ysrc, 0, m, nb, AR2, Kp2, static_cast<__nv_bfloat16*>(y2.p),
+  CANDMC_RET(launch_slice_krow<S>(ysrc, 0, m, nb, AR2, Kp2, static_cast<__nv_bfloat16*>(y2.p),
                                static_cast<int*>(ey2.p), s));
   SliceSrc zsrc{zt.d(), nullptr, nb, kDense, 0};
-  CANDMC_RET(launch_slice_kcol(zsrc, 0, nb, n, BR2, Kp2, (int)Kp2, static_cast<__nv_bfloat16*>(z2.p),
+  CANDMC_RET(launch_slice_kcol<S>(zsrc, 0, nb, n, BR2, Kp2, (int)Kp2, static_cast<__nv_bfloat16*>(z2.p),
                                static_cast<int*>(ez2.p), s));
   OzArgs g2{};
   g2.As = static_cast<__nv_bfloat16*>(y2.p); g2.AR = AR2;
@@ -895,9 +930,30 @@ int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, M
   g2.mode = 1; g2.C = reinterpret_cast<float2*>(C); g2.C64 = C; g2.ldc = ldc;
   g2.Mvalid = m; g2.Nvalid = n; g2.fp64_rows = fp64_rows; g2.status = status;
   g2.c_fp64 = c_fp64 ? 1 : 0;
-  CANDMC_RET(launch_oz(g2, (unsigned)(AR2 / OZ_M), (unsigned)(BR2 / OZ_N), 1, CANDMC_KCLASS_OZ_NN,
+  CANDMC_RET(launch_oz<S>(g2, (unsigned)(AR2 / OZ_M), (unsigned)(BR2 / OZ_N), 1, cls_nn,
                        2.0 * m * n * nb, s));
   return CANDMC_OK;
+}
+
+// The emulated-FP64 form: 7 slices, 28 slice products per K16 step.
+int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
+                   double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
+                   cudaStream_t s, bool c_fp64) {
+  // a panel's own half-panel updates (FP64 storage) are counted apart from
+  // the trailing-matrix contractions
+  return apply_qt_slices<OZ_S>(Y, ldy, ymask, m, nb, Top, C, ldc, n, fp64_rows, status, s, c_fp64,
+                               c_fp64 ? CANDMC_KCLASS_OZ_PANEL : CANDMC_KCLASS_OZ_TN,
+                               c_fp64 ? CANDMC_KCLASS_OZ_PANEL : CANDMC_KCLASS_OZ_NN);
+}
+
+// The FP32 form on the same tensor-core path: 3 BF16 slices (24 bits under
+// each scale group's exponent, FP32-class accuracy), 6 slice products per K16
+// step in 3 accumulator groups, summed in FP32.  C uses the same df64
+// storage as the emulated form.
+int apply_qt_f32(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top, double* C,
+                 int64_t ldc, int64_t n, int64_t fp64_rows, int* status, cudaStream_t s) {
+  return apply_qt_slices<OZ_S32>(Y, ldy, ymask, m, nb, Top, C, ldc, n, fp64_rows, status, s, false,
+                                 CANDMC_KCLASS_F32, CANDMC_KCLASS_F32);
 }
 
 }  // namespace candmc

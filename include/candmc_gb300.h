@@ -62,7 +62,8 @@ const char* candmc_last_error(void);
 #define CANDMC_KCLASS_OZ_SLICE 6    /* Ozaki: FP64 -> BF16 slices */
 #define CANDMC_KCLASS_OZ_TN 7       /* Ozaki: Z = Y^T A on tcgen05 */
 #define CANDMC_KCLASS_OZ_NN 8       /* Ozaki: A -= Y Z on tcgen05 */
-#define CANDMC_KCLASS_F32 9         /* FP32-form contractions */
+#define CANDMC_KCLASS_F32 9         /* FP32-form contractions (3 BF16 slices on tcgen05) */
+#define CANDMC_KCLASS_OZ_PANEL 10   /* emulated-FP64 contractions inside a panel (half-panel updates) */
 long long candmc_launch_count(void);
 int candmc_profile_begin(unsigned mask);
 int candmc_profile_end(int ncls, double* ms, double* work, long long* launches);
@@ -241,18 +242,38 @@ int candmc_QR_Yamamoto_2D_2D(double* A, int64_t lda, int64_t m, int64_t k, int64
                              int compute_Y, double* aQm, int64_t ld_aqm, double* aT, int64_t ld_at,
                              int64_t* agg_n, int64_t* agg_shift, int precision, void* stream);
 
+/* ---- symmetric full -> band reduction: alg/SE/CANSE.h:17-22
+ * (alg/SE/full_to_band.cxx:27-295), the eigensolver's caller of QR_2D_pipe and
+ * compute_invT_from_Y, on a 1 x 1 grid.  A (n x n, ld lda, symmetric, stored
+ * in full, as the reference stores it) becomes Q^T A Q in band form with
+ * bandwidth b: for every
+ * band step the (n - r0 - b) x b block below the band is factored by CAQR in
+ * panels of b_sub (b a multiple of b_sub, b <= 256) and the trailing block
+ * receives the two-sided update A22 -= U V' + (U V')^T (U = Y T^T,
+ * V' = Y^T A22 - (Y^T A22 Y) U^T / 2).  On return the lower triangle holds
+ * the band (diagonal blocks and the R blocks below them) with the reflectors
+ * Y below the band, as the reference leaves them; entries above the diagonal
+ * are not kept up to date.  precision: the form of the panel CAQR's own
+ * trailing updates (the two-sided updates are FP64).  Waits for the stream and
+ * returns the device status. */
+int candmc_sym_full2band(double* A, int64_t lda, int64_t n, int64_t b, int64_t b_sub, int precision,
+                         void* stream);
+
 /* ---- least squares (no counterpart in the reference, which stops at the
  * factorization; built from QR_2D_pipe and update_A) ---------------------------
  * min ||A X - B||_F for A m x n (m >= n, full column rank), B m x nrhs, device
  * pointers.  A is factored in the requested form (a copy; A itself stays
  * resident for the residuals), X0 = R^-1 (Q^T B)[0:n] with Q applied in FP64,
- * then up to max_refine FP64 refinement steps by corrected semi-normal
- * equations (r = B - A X, X += R^-1 R^-T A^T r) until the largest per-column
- * max|dX| / max|X| is <= tol.  The iteration contracts while
- * kappa(A)^2 * u_R < 1 (u_R: the unit roundoff of R's form); a correction
- * that is not smaller than the one before is not applied and ends the
- * refinement.  stats (nullable, 4 doubles): corrections applied, last and
- * first relative correction, device status. */
+ * then up to max_refine FP64 refinement steps of the corrected semi-normal
+ * equations (r = B - A X, X += R^-1 R^-T A^T r), or, with the tuning knob
+ * "ls_refine" = 1, of the augmented system [I A; A^T 0][r; X] = [B; 0]
+ * (Bjorck 1967: f = B - r - A X, g = -A^T r, h = R^-T g, d = Q^T f,
+ * dX = R^-1 (d[0:n] - h), dr = Q [h; d[n:m]]), until the largest per-column max|dX| / max|X| is <= tol.  With R from A's
+ * own QR the iteration contracts by about kappa(A) * u_R per step (u_R: the
+ * unit roundoff of R's form) and stops at the FP64 data's forward-error level,
+ * about kappa(A) * u; a correction that is not smaller than the one before is
+ * not applied and ends the refinement.  stats (nullable, 4 doubles):
+ * corrections applied, last and first relative correction, device status. */
 int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t n, const double* B, int64_t ldb,
                     int64_t nrhs, double* X, int64_t ldx, int64_t b, int precision, int max_refine,
                     double tol, double* stats, void* stream);
@@ -283,7 +304,12 @@ int candmc_batched_status(void* stream, int* status);
  * factors, 32..256, default 128); "panel_oz_min_rows" (in the emulated-FP64
  * form, panels with at least this many rows apply each half's Q^T to the other
  * half of the panel on the tensor cores instead of the FP64 pipe; default
- * 2048, 0 disables) */
+ * 2048, 0 disables); "ls_refine" (candmc_ls_solve's refinement: 0, the
+ * default, the corrected semi-normal equations; 1 the augmented system
+ * [I A; A^T 0] refining x and r); "batched_form" (CANDMC_PREC_FP64, the
+ * default, or CANDMC_PREC_OZAKI: candmc_batched_ls's panels apply each
+ * half-panel's Q^T to the other half on the tensor cores from
+ * "panel_oz_min_rows" rows on) */
 int candmc_set_tuning(const char* key, int64_t value);
 
 /* ---- least-squares request server (no counterpart in the reference) ---------

@@ -208,6 +208,32 @@ int main() {
     for (int64_t c = 0; c < b; ++c) tdiff = std::max(tdiff, fabs(tau[c] - T[c * 16 + (c % 16)]));
     fails += report("tree_tsqr T diagonal vs tau_recon('U')", tdiff, 1e-13);
   }
+  // sym_full2band (the eigensolver's caller of the 2D QR): an orthogonal
+  // similarity onto a band of width b keeps the trace and the Frobenius norm
+  {
+    const int64_t n = 96, b = 16;
+    std::vector<double> A(n * n);
+    for (int64_t c = 0; c < n; ++c)
+      for (int64_t r = 0; r <= c; ++r) A[c * n + r] = A[r * n + c] = fixture(r, c, n, 0.5);
+    double tr0 = 0, f0 = 0;
+    for (int64_t i = 0; i < n * n; ++i) f0 += A[i] * A[i];
+    for (int64_t i = 0; i < n; ++i) tr0 += A[i * n + i];
+    pview pv = candmc_single_gpu_view();
+    sym_full2band(A.data(), n, n, b, 8, &pv);
+    // band matrix from the lower triangle: diagonal blocks and the R blocks below them
+    double tr = 0, f = 0;
+    for (int64_t c = 0; c < n; ++c)
+      for (int64_t r = c; r < n; ++r) {
+        const int64_t blk = c / b, rb = r / b;
+        double v = 0;
+        if (rb == blk) v = A[c * n + r];
+        else if (rb == blk + 1 && (r - (blk + 1) * b) <= (c - blk * b)) v = A[c * n + r];
+        f += (r == c ? 1.0 : 2.0) * v * v;
+        if (r == c) tr += v;
+      }
+    const double d = fabs(tr - tr0) / fabs(tr0) + fabs(sqrt(f) - sqrt(f0)) / sqrt(f0);
+    fails += report("sym_full2band trace + Frobenius norm kept", d, 1e-13);
+  }
   // a grid larger than 1 x 1 is rejected without touching the data
   {
     pview pv = candmc_single_gpu_view();

@@ -41,4 +41,4 @@ def test_dropin_program_passes_reference_criteria(tmp_path):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "TEST FAILED" not in r.stdout
-    assert r.stdout.count("Test successful.") == 11
+    assert r.stdout.count("Test successful.") == 12

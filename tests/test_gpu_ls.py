@@ -96,3 +96,56 @@ def test_ls_solve_ill_conditioned_emulated(cm):
     Xo = co.ls_solve(A, B, 128)
     kappa = 1e10
     assert (np.linalg.norm(X - Xo, axis=0) / np.linalg.norm(Xo, axis=0)).max() <= kappa * 1e-14
+
+
+@pytest.mark.parametrize("refine", [1, 0])
+@pytest.mark.parametrize("prec", ["ozaki", "fp64"])
+def test_ls_kappa_1e10_reaches_the_oracles_forward_error(cm, prec, refine):
+    """sigma from 1 to 1e-10 (kappa = 1e10), inconsistent right-hand sides.
+    No FP64 solver does better than a forward error of order kappa * u = 1e-6
+    on FP64 data: LAPACK's own solution (the oracle) is that far from the exact
+    one.  The refined emulated-FP64 and FP64 solutions must land at that level:
+    within 10 * kappa * u of the oracle's solution, with a normal-equations
+    residual ||A^T r|| / (||A|| ||r||) no larger than the oracle's."""
+    m, n = 2048, 384
+    A = fx.svd_matrix(m, n, 5, 1e-10)
+    B = fx.gaussian(m, 2, 13)
+    Xo = np.linalg.lstsq(A, B, rcond=None)[0]
+    nA = np.linalg.norm(A, 2)
+
+    def eta(X):
+        r = B - A @ X
+        return np.linalg.norm(A.T @ r, axis=0) / (nA * np.linalg.norm(r, axis=0))
+
+    try:
+        cm.set_tuning("ls_refine", refine)
+        X, st = cm.ls_solve(dev(A), dev(B), b=128, precision=prec, max_refine=10, tol=1e-15)
+        torch.cuda.synchronize()
+    finally:
+        cm.set_tuning("ls_refine", 0)
+    X = host(X)
+    assert st["status"] == 0
+    err = np.linalg.norm(X - Xo, axis=0) / np.linalg.norm(Xo, axis=0)
+    assert err.max() <= 10 * 1e10 * 2.2e-16, (err, st)
+    assert (eta(X) <= 2 * eta(Xo)).all(), (eta(X), eta(Xo), st)
+
+
+@pytest.mark.parametrize("smin", [1e-3, 1e-5])
+@pytest.mark.parametrize("refine", [0, 1])
+def test_ls_fp32_form_refined_at_moderate_kappa(cm, smin, refine):
+    """The FP32 form's R (u_R ~ 6e-8) refined in FP64 -- corrected semi-normal
+    equations or the augmented system -- reaches the FP64 oracle's solution up
+    to kappa = 1e5 (contraction ~ kappa * u_R with R from A's own QR)."""
+    m, n = 2000, 256
+    A = fx.svd_matrix(m, n, 3, smin)
+    B = fx.gaussian(m, 2, 17)
+    Xo = np.linalg.lstsq(A, B, rcond=None)[0]
+    try:
+        cm.set_tuning("ls_refine", refine)
+        X, st = cm.ls_solve(dev(A), dev(B), b=128, precision="fp32", max_refine=30, tol=1e-15)
+        torch.cuda.synchronize()
+    finally:
+        cm.set_tuning("ls_refine", 0)
+    X = host(X)
+    err = np.linalg.norm(X - Xo, axis=0) / np.linalg.norm(Xo, axis=0)
+    assert err.max() <= max(LS_TOL, 100 * (1 / smin) * 2.2e-16), (err, st)

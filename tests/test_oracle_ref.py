@@ -201,3 +201,18 @@ def test_reference_tree_and_nlu_match_oracle():
         assert np.array_equal(np.asarray(s1), np.asarray(s2, dtype=np.int64))
         close(A2, A1, b)
         close(R2, R1, b)
+
+
+@pytest.mark.parametrize("n,b,b_sub", [(64, 16, 8), (200, 32, 16), (97, 32, 8)])
+def test_full_to_band_oracle_keeps_the_spectrum(n, b, b_sub):
+    """The restated full -> band reduction (alg/SE/full_to_band.cxx) is an
+    orthogonal similarity onto a band of width b."""
+    from oracle import se_oracle as se
+    X = fx.gaussian(n, n, n)
+    A = np.asfortranarray(X + X.T)
+    Ar = np.array(A, order="F")
+    se.sym_full2band(Ar, b, b_sub)
+    B = se.band_matrix(Ar, b)
+    assert np.abs(np.tril(B, -b - 1)).max() == 0.0
+    ev = np.linalg.eigvalsh(A)
+    assert np.abs(np.linalg.eigvalsh(B) - ev).max() <= 1e-13 * np.abs(ev).max()
