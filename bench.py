@@ -84,6 +84,7 @@ def parse():
     p.add_argument("--no-graph", action="store_true")
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-f32", action="store_true", help="batched: skip the float32-input measurement")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extra", action="store_true",
                    help="caqr: skip the fp64-form, TSQR-HR and precision-form legs")
@@ -865,7 +866,8 @@ def batched_leg(args, ctx):
     a = _sub_args(args, count=4096, seed=3, steps=2, warmup=1, cpu_seconds=10.0)
     ln = wl_batched(a, ctx)
     return {k: ln[k] for k in ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config",
-                               "roofline", "accuracy", "e2e", "cpu_baseline", "clocks", "gpu_launches")}
+                               "roofline", "accuracy", "e2e", "cpu_baseline", "clocks", "gpu_launches",
+                               "float32_inputs")}
 
 
 def serve_leg(args, ctx):
@@ -1005,6 +1007,11 @@ def wl_batched(args, ctx):
         except RuntimeError as ex:
             e2e = {"value": None, "unit": "solves/s", "h2d_bytes_per_step": 8 * (ta + tb),
                    "d2h_bytes_per_step": 8 * xidx.numel(), "error": str(ex)[:200]}
+    f32 = None
+    if not args.no_f32:
+        del As, Bs, Ap, Bp                       # the FP64 copies: room for the float32 run's work area
+        torch.cuda.empty_cache()
+        f32 = batched_f32_inputs(args, ctx, sizes, A0, B0, offA, offB, ta, tb, tuned, use_graph)
     cpu = None
     if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu:
         tasks = [(m, n, 1000 + i) for i, (m, n) in enumerate(sizes)]
@@ -1020,8 +1027,76 @@ def wl_batched(args, ctx):
                       "l2": f"inputs {8 * ta / 1e9:.0f} GB > L2"})
     line.update({"clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
                  "accuracy": {"x_rel_err_vs_lstsq_max": max(errs) if errs else None, "sampled": len(errs),
-                              "bound": 1e-12}})
+                              "bound": 1e-12},
+                 "float32_inputs": f32})
     return line
+
+
+def batched_f32_inputs(args, ctx, sizes, A0, B0, offA, offB, ta, tb, tuned, use_graph):
+    """The same problems stored as float32 (A0, B0 rounded), solved by
+    batched_ls_f32 (widened to FP64 on the device, FP64 solve, x rounded to
+    float32): device-resident solves/s, and end to end with the float32 inputs
+    copied from pinned host memory each step (half the FP64 host traffic)."""
+    import torch
+    cm = ctx.cm
+    count = len(sizes)
+    A32 = torch.empty(ta, dtype=torch.float32, device=ctx.dev)
+    B32 = torch.empty(tb, dtype=torch.float32, device=ctx.dev)
+    A32.copy_(A0)
+    As = [A32[o:o + m * n].view(n, m).t() for o, (m, n) in zip(offA, sizes)]
+    Bs = [B32[o:o + m].view(1, m).t() for o, (m, n) in zip(offB, sizes)]
+    xidx = torch.cat([torch.arange(o, o + n) for o, (m, n) in zip(offB, sizes)]).to(ctx.dev)
+
+    def step():
+        B32.copy_(B0)
+        cm.batched_ls_f32(As, Bs, nstreams=tuned["nstreams"], use_graph=use_graph)
+
+    step()                                        # grows the FP64 work area
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    t_max, launches, _, _ = ctx.timed(step, args.steps, [])
+    out = {"value": ctx.world * count * args.steps / (t_max / 1e3), "unit": "solves/s",
+           "ms_per_step": t_max / args.steps, "gpu_launches": launches}
+    torch.cuda.synchronize()
+    cm.batched_status()
+    rs = np.random.default_rng(1)
+    small = [i for i, (m, n) in enumerate(sizes) if m <= 65536]
+    errs = []
+    for i in rs.choice(small, size=min(8, len(small)), replace=False):
+        m, n = sizes[i]
+        Ah = A32[offA[i]:offA[i] + m * n].view(n, m).t().double().cpu().numpy()
+        bh = B0[offB[i]:offB[i] + m].float().double().cpu().numpy()
+        xo = np.linalg.lstsq(Ah, bh, rcond=None)[0]
+        x = B32[offB[i]:offB[i] + n].double().cpu().numpy()
+        errs.append(float(np.linalg.norm(x - xo) / np.linalg.norm(xo)))
+    out["accuracy"] = {"x_rel_err_vs_lstsq_of_the_float32_data_max": max(errs) if errs else None,
+                       "sampled": len(errs), "bound": 2e-7}
+    if not args.no_e2e:
+        try:
+            hA = torch.empty(ta, dtype=torch.float32, pin_memory=True)
+            hB = torch.empty(tb, dtype=torch.float32, pin_memory=True)
+            hA.copy_(A32)
+            hB.copy_(B0)
+            hx = torch.empty(xidx.numel(), dtype=torch.float32, pin_memory=True)
+            tt = 0.0
+            for it in range(1 + args.steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                A32.copy_(hA, non_blocking=True)
+                B32.copy_(hB, non_blocking=True)
+                cm.batched_ls_f32(As, Bs, nstreams=tuned["nstreams"], use_graph=use_graph)
+                hx.copy_(B32[xidx], non_blocking=True)
+                torch.cuda.synchronize()
+                if it >= 1:
+                    tt += time.perf_counter() - t0
+            out["e2e"] = {"value": ctx.world * count * args.steps / tt, "unit": "solves/s",
+                          "h2d_bytes_per_step": 4 * (ta + tb), "d2h_bytes_per_step": 4 * xidx.numel()}
+            del hA, hB
+        except RuntimeError as ex:
+            out["e2e"] = {"value": None, "error": str(ex)[:200]}
+    del A32, B32
+    return out
 
 
 # ----------------------------------------------------------------- serve

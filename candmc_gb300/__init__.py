@@ -326,6 +326,34 @@ def batched_ls(As, Bs, nstreams=16, use_graph=False, stream=None):
     return [b[:n] for b, n in zip(Bs, ns)]
 
 
+def batched_ls_f32(As, Bs, nstreams=16, use_graph=False, stream=None):
+    """The float32-input variant of batched_ls: A_i (m_i x n_i, column-major
+    float32 CUDA tensors) and b_i (m_i x 1, float32) are solved in FP64; b_i's
+    first n_i entries become x_i (rounded to float32), A_i is left as it was."""
+    import ctypes
+    torch = _torch()
+    k = len(As)
+    arr = lambda t, vals: (t * k)(*vals)
+    for a in As + Bs:
+        if not (isinstance(a, torch.Tensor) and a.is_cuda and a.dtype == torch.float32):
+            raise TypeError("batched_ls_f32: expected float32 CUDA tensors")
+    ms = [a.shape[0] for a in As]
+    ns = [a.shape[1] for a in As]
+    la = []
+    for a in As:
+        if a.stride(0) != 1 and a.shape[0] > 1:
+            raise ValueError("batched_ls_f32: A_i must be column-major")
+        la.append(a.stride(1) if a.shape[1] > 1 else max(1, a.shape[0]))
+    for b in Bs:
+        if b.stride(0) != 1 and b.shape[0] > 1:
+            raise ValueError("batched_ls_f32: b_i must be a contiguous column")
+    check(lib().candmc_batched_ls_f32(k, arr(ctypes.c_int64, ms), arr(ctypes.c_int64, ns),
+                                      arr(ctypes.c_void_p, [a.data_ptr() for a in As]), arr(ctypes.c_int64, la),
+                                      arr(ctypes.c_void_p, [b.data_ptr() for b in Bs]), int(nstreams),
+                                      int(bool(use_graph)), _stream(stream)), "batched_ls_f32")
+    return [b[:n] for b, n in zip(Bs, ns)]
+
+
 def batched_status(stream=None):
     """Wait for the stream and raise CandmcError if a batched call's kernels
     recorded a failure on this device since the last check (then cleared)."""

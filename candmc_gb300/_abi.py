@@ -50,6 +50,7 @@ SIGNATURES = {
     "candmc_ls_solve": [_vp, _i64, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _int, _int,
                         ctypes.c_double, _vp, _vp],
     "candmc_batched_ls": [_i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp],
+    "candmc_batched_ls_f32": [_i64, _vp, _vp, _vp, _vp, _vp, _int, _int, _vp],
     "candmc_set_tuning": [ctypes.c_char_p, _i64],
     "candmc_batched_status": [_vp, _vp],
     "candmc_server_create": [ctypes.c_double, _int, _int, _i64, _int, ctypes.c_double, _vp],

@@ -226,6 +226,8 @@ extern "C" int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t*
   key.push_back(nstreams);
   key.push_back(g_leaf_rows);
   key.push_back(g_pipe_tree);
+  key.push_back(g_batched_form);
+  key.push_back(g_panel_oz_min_rows);
   for (int64_t i = 0; i < nprob; ++i) {
     key.push_back(m[i]);
     key.push_back(n[i]);
@@ -283,5 +285,141 @@ extern "C" int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t*
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   CANDMC_CK(e);
+  return CANDMC_OK;
+}
+
+// ---- float32 inputs --------------------------------------------------------
+// The FP32-input variant of the batched solve: A_i and b_i arrive as float32;
+// they are widened into an FP64 work area on the device, solved exactly as
+// candmc_batched_ls solves FP64 problems (TSQR-HR, Q^T b, back substitution,
+// all FP64), and x_i is rounded back into b_i's first n_i entries.  The work
+// area is kept per device and grows on demand, so repeated calls with the same
+// sizes reuse it (and a captured graph of the FP64 solve stays valid).
+namespace candmc {
+
+__global__ void k_widen_batch(int64_t nprob, const float* const* src, const int64_t* ld, const int64_t* rows,
+                              const int64_t* cols, const int64_t* off, double* dst) {
+  const int64_t p = blockIdx.y;
+  if (p >= nprob) return;
+  const int64_t r = rows[p], c = cols[p], l = ld[p];
+  const float* a = src[p];
+  double* d = dst + off[p];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < r * c; e += (int64_t)gridDim.x * blockDim.x)
+    d[e] = (double)a[(e / r) * l + e % r];
+}
+
+__global__ void k_narrow_x(int64_t nprob, const double* src, const int64_t* off, const int64_t* n,
+                           float* const* dst) {
+  const int64_t p = blockIdx.x;
+  if (p >= nprob) return;
+  for (int64_t e = threadIdx.x; e < n[p]; e += blockDim.x) dst[p][e] = (float)src[off[p] + e];
+}
+
+struct F32Work {
+  double* d = nullptr;
+  size_t cap = 0;      // doubles
+  void* meta = nullptr;
+  size_t meta_cap = 0; // bytes
+  cudaEvent_t done = nullptr;  // end of the last call that used this area
+};
+static F32Work g_f32[64];
+static std::mutex g_f32_mu;
+
+}  // namespace candmc
+
+extern "C" int candmc_batched_ls_f32(int64_t nprob, const int64_t* m, const int64_t* n, float* const* A,
+                                     const int64_t* lda, float* const* B, int nstreams, int use_graph,
+                                     void* stream) {
+  if (nprob < 0 || (nprob > 0 && (!m || !n || !A || !lda || !B)))
+    return set_error(CANDMC_ERR_ARG, "batched_ls_f32 args");
+  for (int64_t i = 0; i < nprob; ++i)
+    if (n[i] < 1 || n[i] > 128 || m[i] < n[i] || lda[i] < m[i] || !A[i] || !B[i])
+      return set_error(CANDMC_ERR_ARG, "batched_ls_f32: each problem needs 1 <= n <= 128 and m >= n");
+  if (nprob == 0) return CANDMC_OK;
+  if (nprob > 65535) return set_error(CANDMC_ERR_ARG, "batched_ls_f32: at most 65535 problems per call");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0;
+  CANDMC_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(CANDMC_ERR_ARG, "device index");
+  // FP64 work area: A_i (m_i x n_i, ld m_i) then b_i (m_i), 32-double aligned
+  std::vector<int64_t> offA(nprob), offB(nprob), ones(nprob, 1), ldw(nprob);
+  size_t tot = 0;
+  for (int64_t i = 0; i < nprob; ++i) {
+    offA[i] = (int64_t)tot;
+    tot += ((size_t)(m[i] * n[i]) + 31) & ~(size_t)31;
+  }
+  for (int64_t i = 0; i < nprob; ++i) {
+    offB[i] = (int64_t)tot;
+    tot += ((size_t)m[i] + 31) & ~(size_t)31;
+    ldw[i] = m[i];
+  }
+  const size_t meta_bytes = sizeof(int64_t) * 8 * (size_t)nprob + sizeof(void*) * 2 * (size_t)nprob;
+  std::lock_guard<std::mutex> lock(g_f32_mu);
+  F32Work& w = g_f32[dev];
+  if (!w.done) CANDMC_CK(cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming));
+  // the previous call may have run on another stream: its solve must finish
+  // before this one rewrites the work area and the tables
+  CANDMC_CK(cudaEventSynchronize(w.done));
+  if (w.cap < tot) {
+    CANDMC_CK(cudaStreamSynchronize(s));
+    if (w.d) cudaFree(w.d);
+    w.d = nullptr;
+    w.cap = 0;
+    CANDMC_CK(cudaMalloc(&w.d, sizeof(double) * tot));
+    w.cap = tot;
+  }
+  if (w.meta_cap < meta_bytes) {
+    CANDMC_CK(cudaStreamSynchronize(s));
+    if (w.meta) cudaFree(w.meta);
+    w.meta = nullptr;
+    w.meta_cap = 0;
+    CANDMC_CK(cudaMalloc(&w.meta, meta_bytes));
+    w.meta_cap = meta_bytes;
+  }
+  // device tables: rows, cols, ld, offsets of A and b, ones, pointers
+  std::vector<unsigned char> h(meta_bytes);
+  int64_t* hi = reinterpret_cast<int64_t*>(h.data());
+  for (int64_t i = 0; i < nprob; ++i) {
+    hi[i] = m[i];
+    hi[nprob + i] = n[i];
+    hi[2 * nprob + i] = lda[i];
+    hi[3 * nprob + i] = offA[i];
+    hi[4 * nprob + i] = offB[i];
+    hi[5 * nprob + i] = 1;
+    hi[6 * nprob + i] = 1;   // ld of b as a column
+  }
+  const float** hp = reinterpret_cast<const float**>(h.data() + sizeof(int64_t) * 8 * nprob);
+  for (int64_t i = 0; i < nprob; ++i) {
+    hp[i] = A[i];
+    hp[nprob + i] = B[i];
+  }
+  CANDMC_CK(cudaMemcpyAsync(w.meta, h.data(), meta_bytes, cudaMemcpyHostToDevice, s));
+  CANDMC_CK(cudaStreamSynchronize(s));   // h is pageable and goes out of scope
+  const int64_t* dm = static_cast<const int64_t*>(w.meta);
+  const int64_t* dn = dm + nprob;
+  const int64_t* dl = dm + 2 * nprob;
+  const int64_t* doA = dm + 3 * nprob;
+  const int64_t* doB = dm + 4 * nprob;
+  const int64_t* d1 = dm + 5 * nprob;
+  const float* const* dpA = reinterpret_cast<const float* const*>(static_cast<char*>(w.meta) + sizeof(int64_t) * 8 * nprob);
+  const float* const* dpB = dpA + nprob;
+  {
+    ProfScope ps(CANDMC_KCLASS_SMALL, 12.0 * (double)tot, s);
+    k_widen_batch<<<dim3(256, (unsigned)nprob), 256, 0, s>>>(nprob, dpA, dl, dm, dn, doA, w.d);
+    k_widen_batch<<<dim3(64, (unsigned)nprob), 256, 0, s>>>(nprob, dpB, dm, dm, d1, doB, w.d);
+  }
+  CANDMC_CK(cudaGetLastError());
+  std::vector<double*> Ad(nprob), Bd(nprob);
+  for (int64_t i = 0; i < nprob; ++i) {
+    Ad[i] = w.d + offA[i];
+    Bd[i] = w.d + offB[i];
+  }
+  CANDMC_RET(candmc_batched_ls(nprob, m, n, Ad.data(), ldw.data(), Bd.data(), nstreams, use_graph, s));
+  {
+    ProfScope ps(CANDMC_KCLASS_SMALL, 0.0, s);
+    k_narrow_x<<<(unsigned)nprob, 128, 0, s>>>(nprob, w.d, doB, dn, const_cast<float* const*>(dpB));
+  }
+  CANDMC_CK(cudaGetLastError());
+  CANDMC_CK(cudaEventRecord(w.done, s));
   return CANDMC_OK;
 }

@@ -289,6 +289,17 @@ int candmc_ls_solve(const double* A, int64_t lda, int64_t m, int64_t n, const do
 int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t* n, double* const* A,
                       const int64_t* lda, double* const* B, int nstreams, int use_graph, void* stream);
 
+/* candmc_batched_ls_f32: the float32-input variant (no counterpart in the
+ * reference): A_i (ld lda_i) and b_i are float32; they are widened into an
+ * FP64 work area on the device (kept per device, grown on demand, released at
+ * exit), solved by candmc_batched_ls in FP64, and x_i is rounded into the
+ * first n_i entries of b_i (A_i is left as it was).  At most 65535 problems per
+ * call.  The host waits for the previous call on this device to finish (the
+ * work area is shared) and synchronises the stream once to upload the problem
+ * tables. */
+int candmc_batched_ls_f32(int64_t nprob, const int64_t* m, const int64_t* n, float* const* A,
+                          const int64_t* lda, float* const* B, int nstreams, int use_graph, void* stream);
+
 /* candmc_batched_status: waits for the stream, then returns in *status the
  * first failure any batched call's kernels recorded on this device since the
  * last call (CANDMC_OK if none: e.g. CANDMC_ERR_TIMEOUT, CANDMC_ERR_NUMERIC)

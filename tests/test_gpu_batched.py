@@ -92,3 +92,43 @@ def test_leaf_rows_tuning_keeps_results(cm, m_lo, m_hi):
         torch.cuda.synchronize()
         check(host, xs)
     cm.set_tuning("leaf_rows", 64)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batched_float32_inputs(cm, use_graph):
+    """The float32-input variant: A_i, b_i stored as float32, solved in FP64;
+    x_i (rounded to float32) within float32 rounding of LAPACK's solution of
+    the same float32 data in float64, and A_i left as it was."""
+    host = make(fx.batched_problems(40, seed=7, m_lo=128, m_hi=8192))
+    host32 = [(A.astype(np.float32), b.astype(np.float32)) for A, b in host]
+    As = [torch.from_numpy(np.asfortranarray(A)).cuda().t().contiguous().t() for A, _ in host32]
+    Bs = [torch.from_numpy(np.asfortranarray(b)).cuda().t().contiguous().t() for _, b in host32]
+    A_before = [a.clone() for a in As]
+    for _ in range(2):     # twice: the graph path captures, then replays
+        for b, (_, bh) in zip(Bs, host32):
+            b.copy_(torch.from_numpy(np.asfortranarray(bh)).cuda())
+        xs = cm.batched_ls_f32(As, Bs, nstreams=8, use_graph=use_graph)
+        torch.cuda.synchronize()
+        cm.batched_status()
+        for (A, b), x in zip(host32, xs):
+            xo = np.linalg.lstsq(A.astype(np.float64), b.astype(np.float64), rcond=None)[0]
+            err = np.linalg.norm(x.cpu().numpy().astype(np.float64) - xo) / np.linalg.norm(xo)
+            assert err <= 2e-7, err
+    for a, a0 in zip(As, A_before):
+        assert torch.equal(a, a0)
+
+
+def test_batched_emulated_panel_form(cm):
+    """batched_form = emulated FP64: the panels' half-panel updates on the
+    tensor cores for panels of at least panel_oz_min_rows rows; same 1e-12 bar."""
+    host = make(fx.batched_problems(24, seed=9, m_lo=2048, m_hi=65536))
+    As, Bs = to_dev(host)
+    try:
+        cm.set_tuning("batched_form", 1)
+        cm.set_tuning("panel_oz_min_rows", 1024)
+        xs = cm.batched_ls(As, Bs, nstreams=8)
+        torch.cuda.synchronize()
+    finally:
+        cm.set_tuning("batched_form", 0)
+        cm.set_tuning("panel_oz_min_rows", 2048)
+    check(host, xs)
