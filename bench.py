@@ -85,6 +85,7 @@ def parse():
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-f32", action="store_true", help="batched: skip the float32-input measurement")
+    p.add_argument("--no-extra-forms", action="store_true", help="batched: skip the plain-FP64 comparison")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extra", action="store_true",
                    help="caqr: skip the fp64-form, TSQR-HR and precision-form legs")
@@ -867,7 +868,7 @@ def batched_leg(args, ctx):
     ln = wl_batched(a, ctx)
     return {k: ln[k] for k in ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config",
                                "roofline", "accuracy", "e2e", "cpu_baseline", "clocks", "gpu_launches",
-                               "float32_inputs")}
+                               "fp64_form", "float32_inputs")}
 
 
 def serve_leg(args, ctx):
@@ -953,6 +954,21 @@ def wl_batched(args, ctx):
     classes = ["panel_leaf", "panel_y", "small", "gemm_tn", "gemm_nn", "reduce"]
     t_max, launches, prof, clk = ctx.timed(step, args.steps, classes)
     solves = ctx.world * count * args.steps / (t_max / 1e3)
+    # plain FP64 beside the chosen form: the same problems with the panels'
+    # half-panel updates on the FP64 pipe (batched_form 0)
+    fp64_form = None
+    if not args.no_extra_forms:
+        cm.set_tuning("batched_form", 0)
+        try:
+            step()
+            torch.cuda.synchronize()
+            t64, l64, _, _ = ctx.timed(step, args.steps, [])
+            fp64_form = {"value": ctx.world * count * args.steps / (t64 / 1e3), "unit": "solves/s",
+                         "ms_per_step": t64 / args.steps, "gpu_launches": l64,
+                         "form": "half-panel updates on the FP64 pipe (batched_form 0)"}
+        finally:
+            cm.set_tuning("batched_form", 1)
+        step()                                   # the chosen form's result for the accuracy check
     f = sum(qr_flops(m, n) for m, n in sizes)
     by = sum(16.0 * m * n for m, n in sizes)
     roof = fp64_roof(prof, ["panel_leaf", "panel_y"], "k_hr6_pipe / k_hr4_leaf_tree + k_hr4_form_y", t_max)
@@ -1024,11 +1040,13 @@ def wl_batched(args, ctx):
                      {"workload": f"{count} LS problems, m log-uniform [256, 262144], n in "
                                   "{8,16,32,64,128}, A,b ~ N(0,1) on the device (Philox seed 3)",
                       "problems": count, "tuning": tuned, "graph": use_graph,
+                      "form": "half-panel updates of panels >= 2048 rows in emulated FP64 on tcgen05 "
+                              "(batched_form 1), everything else FP64",
                       "l2": f"inputs {8 * ta / 1e9:.0f} GB > L2"})
     line.update({"clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
                  "accuracy": {"x_rel_err_vs_lstsq_max": max(errs) if errs else None, "sampled": len(errs),
                               "bound": 1e-12},
-                 "float32_inputs": f32})
+                 "fp64_form": fp64_form, "float32_inputs": f32})
     return line
 
 

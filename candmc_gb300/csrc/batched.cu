@@ -65,9 +65,9 @@ static int batched_status_word(int dev, int** out) {
   return CANDMC_OK;
 }
 // arithmetic form of the panels' own half-panel updates in batched calls
-// (tuning knob "batched_form"): FP64, or emulated FP64 on the tensor cores
-// for panels of at least "panel_oz_min_rows" rows
-int g_batched_form = CANDMC_PREC_FP64;
+// (tuning knob "batched_form"): emulated FP64 on the tensor cores for panels
+// of at least "panel_oz_min_rows" rows (the default), or FP64
+int g_batched_form = CANDMC_PREC_OZAKI;
 static std::mutex g_graph_mu;
 struct CachedGraph {
   cudaGraphExec_t exec;

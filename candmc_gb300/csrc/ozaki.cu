@@ -439,6 +439,37 @@ __device__ __forceinline__ bool oz_wait(uint64_t* b, uint32_t parity, volatile i
   return false;
 }
 
+// One 128 x 96 x 16 BF16 MMA into the accumulator at TMEM column address dt;
+// accum = 0 overwrites it.
+__device__ __forceinline__ void umma_bf16(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc,
+                                          uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+}
+
+// The slice-pair MMAs of one K16 step.  da / db: descriptors of the stage's
+// first A and B slice (the slices follow at fixed byte strides, and a
+// descriptor's address field is the shared-memory address / 16, so slice
+// descriptors are the base plus a constant).  In loop order the first product
+// of accumulator group g is (0, g): in a group's first step (FIRST) those
+// overwrite their accumulator, every other product adds to it.
+template <int S, int G, bool FIRST>
+__device__ __forceinline__ void oz_issue_step(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc) {
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      if (i + j >= S) continue;
+      const int g = (i + j < G - 1) ? i + j : G - 1;
+      const bool first = FIRST && i == 0 && j < G;
+      umma_bf16(tmem + (uint32_t)(g * OZ_N), da + (uint64_t)(i * (OZ_ABYTES >> 4)),
+                db + (uint64_t)(j * (OZ_BBYTES >> 4)), idesc, first ? 0u : 1u);
+    }
+  }
+}
+
 // Work item w of a launch: (M tile, N tile, K range).  M tiles run fastest so
 // that consecutive items of a CTA share the B operand's slices in L2.
 struct OzItem {
@@ -530,6 +561,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
     if (lane == 0) {
       const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_N >> 3) << 17) |
                              ((uint32_t)(OZ_M >> 4) << 24);
+      // ring stages are 1024-byte aligned and the ring ends below 256 KB, so
+      // base + offset / 16 stays inside the descriptor's 14-bit address field
+      const uint64_t ring_desc = make_desc(smem_u32(ring));
+      static_assert((OZ_STAGES * STAGE_BYTES + 2048) < (1 << 18), "ring within the descriptor's range");
+      static_assert(STAGE_BYTES % 16 == 0 && OZ_ABYTES % 16 == 0 && OZ_BBYTES % 16 == 0, "16-byte strides");
       int64_t gs = 0, ngroups = 0;
       for (int64_t w = blockIdx.x; w < nitems && !s_fail; w += gridDim.x) {
         const OzItem it = oz_item(a, w);
@@ -543,28 +579,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
           const int st = (int)(gs % OZ_STAGES);
           if (!oz_wait(&full_b[st], (uint32_t)((gs / OZ_STAGES) & 1), &s_fail)) break;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          unsigned char* sb = ring + (size_t)st * STAGE_BYTES;
-          // the first product into each accumulator in a group's first step overwrites it
-          bool first_of_group[G];
-#pragma unroll
-          for (int g = 0; g < G; ++g) first_of_group[g] = (sig == 0);
-#pragma unroll
-          for (int i = 0; i < S; ++i) {
-#pragma unroll
-            for (int j = 0; j < S; ++j) {
-              if (i + j >= S) continue;
-              const int g = (i + j < G - 1) ? i + j : G - 1;
-              const uint64_t ad = make_desc(smem_u32(sb + i * OZ_ABYTES));
-              const uint64_t bd = make_desc(smem_u32(sb + S * OZ_ABYTES + j * OZ_BBYTES));
-              const uint32_t dt = tmem + (uint32_t)(g * OZ_N);
-              const uint32_t accum = first_of_group[g] ? 0u : 1u;
-              first_of_group[g] = false;
-              asm volatile(
-                  "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
-                  "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
-            }
-          }
+          const uint64_t da = ring_desc + (uint64_t)(st * (STAGE_BYTES >> 4));
+          const uint64_t db = da + (uint64_t)((S * OZ_ABYTES) >> 4);
+          if (sig == 0)
+            oz_issue_step<S, G, true>(tmem, da, db, idesc);
+          else
+            oz_issue_step<S, G, false>(tmem, da, db, idesc);
           // the stage is free once these MMAs have read it
           asm volatile(
               "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(

@@ -317,10 +317,10 @@ int candmc_batched_status(void* stream, int* status);
  * half of the panel on the tensor cores instead of the FP64 pipe; default
  * 2048, 0 disables); "ls_refine" (candmc_ls_solve's refinement: 0, the
  * default, the corrected semi-normal equations; 1 the augmented system
- * [I A; A^T 0] refining x and r); "batched_form" (CANDMC_PREC_FP64, the
- * default, or CANDMC_PREC_OZAKI: candmc_batched_ls's panels apply each
- * half-panel's Q^T to the other half on the tensor cores from
- * "panel_oz_min_rows" rows on) */
+ * [I A; A^T 0] refining x and r); "batched_form" (CANDMC_PREC_OZAKI, the
+ * default: candmc_batched_ls's panels apply each half-panel's Q^T to the
+ * other half on the tensor cores from "panel_oz_min_rows" rows on, in
+ * emulated FP64 on FP64 storage; CANDMC_PREC_FP64: on the FP64 pipe) */
 int candmc_set_tuning(const char* key, int64_t value);
 
 /* ---- least-squares request server (no counterpart in the reference) ---------

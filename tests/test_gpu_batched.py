@@ -118,17 +118,19 @@ def test_batched_float32_inputs(cm, use_graph):
         assert torch.equal(a, a0)
 
 
-def test_batched_emulated_panel_form(cm):
-    """batched_form = emulated FP64: the panels' half-panel updates on the
-    tensor cores for panels of at least panel_oz_min_rows rows; same 1e-12 bar."""
+@pytest.mark.parametrize("form", [0, 1])
+def test_batched_panel_forms(cm, form):
+    """batched_form 1 (the default): the panels' half-panel updates in emulated
+    FP64 on the tensor cores for panels of at least panel_oz_min_rows rows;
+    batched_form 0: on the FP64 pipe.  Same 1e-12 bar for both."""
     host = make(fx.batched_problems(24, seed=9, m_lo=2048, m_hi=65536))
     As, Bs = to_dev(host)
     try:
-        cm.set_tuning("batched_form", 1)
+        cm.set_tuning("batched_form", form)
         cm.set_tuning("panel_oz_min_rows", 1024)
         xs = cm.batched_ls(As, Bs, nstreams=8)
         torch.cuda.synchronize()
     finally:
-        cm.set_tuning("batched_form", 0)
+        cm.set_tuning("batched_form", 1)
         cm.set_tuning("panel_oz_min_rows", 2048)
     check(host, xs)
