@@ -96,22 +96,29 @@ int hr_rec(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, int
   const int b1 = b / 2, b2 = b - b1;
   CANDMC_RET(hr_rec(A, lda, m, b1, T, ldT, st, precision, s));
   // Q1^T on the right half.  The reflectors, norms, tree and T stay FP64;
-  // this m x b/2 x b/2 product is a trailing update, so in the emulated-FP64
-  // form (and on tall panels, where its FP64 cost is on the panel's critical
-  // path) it runs on the tensor cores with the panel kept in FP64 storage.
-  if (precision == CANDMC_PREC_OZAKI && g_panel_oz_min_rows > 0 && m >= g_panel_oz_min_rows)
+  // this m x b/2 x b/2 product is a trailing update, so in the tensor-core
+  // forms (emulated FP64, and FP32, whose panels keep FP64-class accuracy) on
+  // tall panels, where its FP64 cost is on the panel's critical path, it runs
+  // in emulated FP64 on the tensor cores with the panel kept in FP64 storage.
+  const bool oz = precision != CANDMC_PREC_FP64 && g_panel_oz_min_rows > 0 && m >= g_panel_oz_min_rows;
+  if (oz)
     CANDMC_RET(apply_qt_ozaki(A, lda, kUnitLower, m, b1, mref(T, ldT, 1, kUpper), A + (int64_t)b1 * lda,
                               lda, b2, m, st, s, true));
   else
     CANDMC_RET(apply_qt(A, lda, m, b1, T, ldT, A + (int64_t)b1 * lda, lda, b2, CANDMC_PREC_FP64, s));
   double* T22 = T + (int64_t)b1 * ldT + b1;
   CANDMC_RET(hr_rec(A + (int64_t)b1 * lda + b1, lda, m - b1, b2, T22, ldT, st, precision, s));
-  // G = Y1[b1:m, :]^T * Y2   (Y2 unit-lower in A[b1:, b1:])
+  // G = Y1[b1:m, :]^T * Y2   (Y2 unit-lower in A[b1:, b1:]); with the half
+  // update on the tensor cores, this (m - b1) x b1 x b2 product goes there too
   DevBuf g, x;
   CANDMC_RET(g.alloc(sizeof(double) * b1 * b2, s));
   CANDMC_RET(x.alloc(sizeof(double) * b1 * b2, s));
-  CANDMC_RET(gemm_tn_reduce(mref(A + b1, lda), mref(A + (int64_t)b1 * lda + b1, lda, 0, kUnitLower),
-                            m - b1, b1, b2, mref(nullptr, 0), 1.0, g.d(), b1, s));
+  if (oz)
+    CANDMC_RET(gram_ozaki(A + b1, lda, kDense, A + (int64_t)b1 * lda + b1, lda, kUnitLower, m - b1, b1, b2,
+                          g.d(), st, s));
+  else
+    CANDMC_RET(gemm_tn_reduce(mref(A + b1, lda), mref(A + (int64_t)b1 * lda + b1, lda, 0, kUnitLower),
+                              m - b1, b1, b2, mref(nullptr, 0), 1.0, g.d(), b1, s));
   // X = T11 * G;  T12 = -X * T22
   CANDMC_RET(small_gemm(b1, b2, b1, 1.0, mref(T, ldT, 0, kUpper), mref(g.d(), b1), 0.0, x.d(), b1, s));
   CANDMC_RET(small_gemm(b1, b2, b2, -1.0, mref(x.d(), b1), mref(T22, ldT, 0, kUpper), 0.0,

@@ -71,9 +71,10 @@ int larft_from_gram(const double* G, int64_t ldg, const double* tau, int b, doub
 int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
                    double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
                    cudaStream_t s, bool c_fp64 = false);
-// rows from which hr_rec applies a half panel's Q^T to the other half with the
-// emulated-FP64 contraction when the factorization runs in that form (tuning
-// knob "panel_oz_min_rows"; 0 disables)
+// rows from which hr_rec applies a half panel's Q^T to the other half, and
+// forms the Gram product of its T merge, with the emulated-FP64 contraction
+// when the factorization runs in a tensor-core form (emulated FP64 or FP32;
+// tuning knob "panel_oz_min_rows"; 0 disables)
 extern int64_t g_panel_oz_min_rows;
 // least-squares refinement: 0 corrected semi-normal equations (default), 1
 // augmented system (tuning knob "ls_refine")
@@ -82,6 +83,9 @@ extern int g_ls_refine;
 // accumulation; df64 storage of C).
 int apply_qt_f32(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top, double* C,
                  int64_t ldc, int64_t n, int64_t fp64_rows, int* status, cudaStream_t s);
+// G (nb x n, ld nb) = Y^T C for FP64 operands read through masks, in emulated FP64
+int gram_ozaki(const double* Y, int64_t ldy, int ymask, const double* C, int64_t ldc, int cmask, int64_t m,
+               int nb, int64_t n, double* G, int* status, cudaStream_t s);
 int to_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
 int from_df64(double* X, int64_t ld, int64_t m, int64_t n, cudaStream_t s);
 

@@ -399,6 +399,22 @@ __device__ __forceinline__ f2 df_add_sloppy(f2 x, f2 y) {
   return {h, __fsub_rn(l, __fsub_rn(h, s))};
 }
 
+// Accumulation of the epilogue: df64 for the emulated-FP64 form (G = 5); for
+// the FP32 form (G < 5, products accurate to FP32) plain FP32, which keeps C
+// in the df64 slots with a zero low word.
+template <int G>
+__device__ __forceinline__ f2 oz_accumulate(f2 x, f2 y) {
+  if constexpr (G == 5) return df_add_sloppy(x, y);
+  else return {__fadd_rn(x.h, y.h), 0.0f};
+}
+
+// C - p for the read-modify-write of MODE 1 (same split by form)
+template <int G>
+__device__ __forceinline__ f2 oz_subtract(f2 c, f2 p) {
+  if constexpr (G == 5) return df_add(c, {-p.h, -p.l});
+  else return {__fsub_rn(__fadd_rn(c.h, c.l), p.h), 0.0f};
+}
+
 __device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
 }
@@ -676,7 +692,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
               const f2 v = combine_g<G>(gv, j);
               const float f = pow2f(eA + eB[j] - 16);
               const f2 sv = {__fmul_rn(v.h, f), __fmul_rn(v.l, f)};
-              if (MODE == 0) acc[c8 * 8 + j] = df_add_sloppy(acc[c8 * 8 + j], sv);
+              if (MODE == 0) acc[c8 * 8 + j] = oz_accumulate<G>(acc[c8 * 8 + j], sv);
               else acc[c8 * 8 + j] = sv;
             }
           } else {
@@ -690,7 +706,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
               const float f1 = pow2f(e1), f2v = pow2f(e2), f3 = pow2f(e - e1 - e2);
               const f2 sv = {__fmul_rn(__fmul_rn(__fmul_rn(v.h, f1), f2v), f3),
                              __fmul_rn(__fmul_rn(__fmul_rn(v.l, f1), f2v), f3)};
-              if (MODE == 0) acc[c8 * 8 + j] = df_add_sloppy(acc[c8 * 8 + j], sv);
+              if (MODE == 0) acc[c8 * 8 + j] = oz_accumulate<G>(acc[c8 * 8 + j], sv);
               else acc[c8 * 8 + j] = sv;
             }
           }
@@ -730,7 +746,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
               const int64_t gn = it.n0 + part * OZ_EPI_COLS + c16 * 16 + j;
               if (gn >= a.Nvalid) continue;
               const int64_t ci = gn * a.ldc + gm;
-              const f2 r = df_add({cv[j].x, cv[j].y}, {-acc[c16 * 16 + j].h, -acc[c16 * 16 + j].l});
+              const f2 r = oz_subtract<G>({cv[j].x, cv[j].y}, acc[c16 * 16 + j]);
               if (gm < a.fp64_rows) a.C64[ci] = df_to_double(r);
               else a.C[ci] = make_float2(r.h, r.l);
             }
@@ -877,33 +893,23 @@ static int launch_oz(OzArgs a, unsigned gm, unsigned gn, unsigned gk, int cls, d
   return CANDMC_OK;
 }
 
-// The trailing update with S-slice contractions: C <- C - Y (Top (Y^T C)).
-// C (m x n, ld ldc) holds df64 pairs; rows < fp64_rows of C are written back
-// as FP64 (finished R rows).  With c_fp64, C is FP64 storage instead (read and
-// written as FP64).  Y: unit-lower m x nb (read from a Y\R buffer, FP64),
-// Top: the nb x nb operator applied to Y^T C.  cls_tn / cls_nn: the kernel
-// classes the two contractions are counted under.
+// Z (nb x n, FP64, ld nb) = Y^T C with S-slice contractions: Y (m x nb) and C
+// (m x n) read through their slice sources; split-K partials summed in df64.
 template <int S>
-static int apply_qt_slices(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
-                           double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
-                           cudaStream_t s, bool c_fp64, int cls_tn, int cls_nn) {
-  if (m <= 0 || n <= 0) return CANDMC_OK;
-  if (nb > OZ_M) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
+static int oz_tn(const SliceSrc& ysrc, const SliceSrc& csrc, int64_t m, int nb, int64_t n, double* Z,
+                 int* status, cudaStream_t s, int cls) {
   const int64_t KG = 128;                       // K rows per exact accumulation
-  // ---- GEMM1: Z = Y^T C.  A-op = Y^T (rows = Householder index, K = m), B-op = C (rows = columns)
+  // A-op = Y^T (rows = Householder index, K = m), B-op = C (rows = columns)
   const int64_t Kp1 = rup(m, KG);
   const int64_t AR1 = OZ_M, BR1 = rup(n, OZ_N);
-  DevBuf ya, ea, cb, eb, part, z;
+  DevBuf ya, ea, cb, eb, part;
   CANDMC_RET(ya.alloc(sizeof(__nv_bfloat16) * S * AR1 * Kp1, s));
   CANDMC_RET(ea.alloc(sizeof(int) * (Kp1 / KG) * AR1, s));
   CANDMC_RET(cb.alloc(sizeof(__nv_bfloat16) * S * BR1 * Kp1, s));
   CANDMC_RET(eb.alloc(sizeof(int) * (Kp1 / KG) * BR1, s));
-  SliceSrc ysrc{Y, nullptr, ldy, ymask, 0};
   auto* yas = static_cast<__nv_bfloat16*>(ya.p);
   auto* cbs = static_cast<__nv_bfloat16*>(cb.p);
   CANDMC_RET(launch_slice_kcol<S>(ysrc, 0, m, nb, AR1, Kp1, (int)KG, yas, static_cast<int*>(ea.p), s));
-  SliceSrc csrc = c_fp64 ? SliceSrc{C, nullptr, ldc, kDense, 0}
-                         : SliceSrc{nullptr, reinterpret_cast<const float2*>(C), ldc, kDense, 0};
   CANDMC_RET(launch_slice_kcol<S>(csrc, 0, m, n, BR1, Kp1, (int)KG, cbs, static_cast<int*>(eb.p), s));
   // K split: about two waves of CTAs
   const int64_t ntiles = BR1 / OZ_N;
@@ -916,18 +922,35 @@ static int apply_qt_slices(const double* Y, int64_t ldy, int ymask, int64_t m, i
   g1.kgroup = KG; g1.eA = static_cast<int*>(ea.p); g1.eB = static_cast<int*>(eb.p);
   g1.mode = 0; g1.part = static_cast<float2*>(part.p); g1.Mvalid = nb; g1.Nvalid = n;
   g1.status = status;
-  CANDMC_RET(launch_oz<S>(g1, 1, (unsigned)ntiles, (unsigned)ksplit, cls_tn,
-                       2.0 * nb * n * m, s));
-  // ---- Z' = T^T * sum(partials)   (FP64, nb x n)
+  CANDMC_RET(launch_oz<S>(g1, 1, (unsigned)ntiles, (unsigned)ksplit, cls, 2.0 * nb * n * m, s));
+  ProfScope ps(CANDMC_KCLASS_REDUCE, 8.0 * ksplit * n * AR1, s);
+  k_oz_sum_partials<<<(unsigned)((nb * n + 255) / 256), 256, 0, s>>>(static_cast<float2*>(part.p),
+                                                                      (int)ksplit, AR1, nb, n, Z);
+  CANDMC_CK(cudaGetLastError());
+  return CANDMC_OK;
+}
+
+// The trailing update with S-slice contractions: C <- C - Y (Top (Y^T C)).
+// C (m x n, ld ldc) holds df64 pairs; rows < fp64_rows of C are written back
+// as FP64 (finished R rows).  With c_fp64, C is FP64 storage instead (read and
+// written as FP64).  Y: unit-lower m x nb (read from a Y\R buffer, FP64),
+// Top: the nb x nb operator applied to Y^T C.  cls_tn / cls_nn: the kernel
+// classes the two contractions are counted under.
+template <int S>
+static int apply_qt_slices(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top,
+                           double* C, int64_t ldc, int64_t n, int64_t fp64_rows, int* status,
+                           cudaStream_t s, bool c_fp64, int cls_tn, int cls_nn) {
+  if (m <= 0 || n <= 0) return CANDMC_OK;
+  if (nb > OZ_M) return set_error(CANDMC_ERR_ARG, "ozaki form needs b <= 128");
+  // ---- GEMM1: Z = Y^T C
+  SliceSrc ysrc{Y, nullptr, ldy, ymask, 0};
+  SliceSrc csrc = c_fp64 ? SliceSrc{C, nullptr, ldc, kDense, 0}
+                         : SliceSrc{nullptr, reinterpret_cast<const float2*>(C), ldc, kDense, 0};
+  DevBuf z, zt;
   CANDMC_RET(z.alloc(sizeof(double) * nb * n, s));
-  DevBuf zt;
+  CANDMC_RET(oz_tn<S>(ysrc, csrc, m, nb, n, z.d(), status, s, cls_tn));
+  // ---- Z' = T^T * Z   (FP64, nb x n)
   CANDMC_RET(zt.alloc(sizeof(double) * nb * n, s));
-  {
-    ProfScope ps(CANDMC_KCLASS_REDUCE, 8.0 * ksplit * n * AR1, s);
-    k_oz_sum_partials<<<(unsigned)((nb * n + 255) / 256), 256, 0, s>>>(
-        static_cast<float2*>(part.p), (int)ksplit, AR1, nb, n, z.d());
-    CANDMC_CK(cudaGetLastError());
-  }
   CANDMC_RET(small_gemm(nb, n, nb, 1.0, Top, mref(z.d(), nb), 0.0, zt.d(), nb, s));
   // ---- GEMM2: C -= Y * Z'.  A-op = Y (rows = m, K = nb), B-op = Z'^T (rows = columns, K = nb)
   const int64_t Kp2 = rup(nb, 16);
@@ -968,12 +991,25 @@ int apply_qt_ozaki(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, M
 
 // The FP32 form on the same tensor-core path: 3 BF16 slices (24 bits under
 // each scale group's exponent, FP32-class accuracy), 6 slice products per K16
-// step in 3 accumulator groups, summed in FP32.  C uses the same df64
-// storage as the emulated form.
+// step in 3 accumulator groups, summed in FP32.  C keeps the df64 slots of
+// the emulated form, but the epilogue updates it in FP32 arithmetic (its low
+// word becomes zero), so the read-modify-write costs one FP32 operation per
+// element instead of a df64 addition.
 int apply_qt_f32(const double* Y, int64_t ldy, int ymask, int64_t m, int nb, MatRef Top, double* C,
                  int64_t ldc, int64_t n, int64_t fp64_rows, int* status, cudaStream_t s) {
   return apply_qt_slices<OZ_S32>(Y, ldy, ymask, m, nb, Top, C, ldc, n, fp64_rows, status, s, false,
                                  CANDMC_KCLASS_F32, CANDMC_KCLASS_F32);
+}
+
+// G (nb x n, FP64, ld nb) = Y^T C for FP64 Y (m x nb, mask ymask) and C
+// (m x n, mask cmask) in emulated FP64: the Gram product of a panel's
+// recursive T merge.
+int gram_ozaki(const double* Y, int64_t ldy, int ymask, const double* C, int64_t ldc, int cmask, int64_t m,
+               int nb, int64_t n, double* G, int* status, cudaStream_t s) {
+  if (m <= 0 || n <= 0 || nb <= 0) return CANDMC_OK;
+  if (nb > OZ_M) return set_error(CANDMC_ERR_ARG, "gram_ozaki needs nb <= 128");
+  return oz_tn<OZ_S>(SliceSrc{Y, nullptr, ldy, ymask, 0}, SliceSrc{C, nullptr, ldc, cmask, 0}, m, nb, n, G,
+                     status, s, CANDMC_KCLASS_OZ_PANEL);
 }
 
 }  // namespace candmc

@@ -223,6 +223,12 @@ extern "C" int64_t candmc_ls_request_bytes(int64_t m, int64_t n, int64_t b, int 
   by += 8 * (300 * m + 8 * b * b);
   // refinement products: split-K partials of A x (row tiles) and A^T r
   by += 8 * (m + 4 * 152 * 128 + 4 * 152 * n);
+  if (precision != CANDMC_PREC_FP64 && g_panel_oz_min_rows > 0 && m >= g_panel_oz_min_rows) {
+    // the panels' emulated-FP64 half-panel updates and Gram products: seven
+    // BF16 planes of both operands (128 + 96 padded rows) per row of the
+    // panel, and the split-K partials (at most two waves of CTAs)
+    by += 2 * 7 * (128 + 96) * m + 8 * 128 * b * 2 * 152;
+  }
   if (n > b) {
     // trailing update: BF16 slices / FP32 copies / split-K partials of the
     // contraction over the trailing columns
