@@ -1040,7 +1040,7 @@ def wl_batched(args, ctx):
                      {"workload": f"{count} LS problems, m log-uniform [256, 262144], n in "
                                   "{8,16,32,64,128}, A,b ~ N(0,1) on the device (Philox seed 3)",
                       "problems": count, "tuning": tuned, "graph": use_graph,
-                      "form": "half-panel updates of panels >= 2048 rows in emulated FP64 on tcgen05 "
+                      "form": "half-panel updates and Gram products of panels >= 8192 rows in emulated FP64 on tcgen05 "
                               "(batched_form 1), everything else FP64",
                       "l2": f"inputs {8 * ta / 1e9:.0f} GB > L2"})
     line.update({"clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,

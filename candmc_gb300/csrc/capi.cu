@@ -23,7 +23,7 @@ namespace candmc {
 
 static thread_local std::string g_last_error;
 
-int64_t g_panel_oz_min_rows = 2048;
+int64_t g_panel_oz_min_rows = 8192;
 
 int set_error(int code, const char* what) {
   g_last_error = what ? what : "";

@@ -315,7 +315,7 @@ int candmc_batched_status(void* stream, int* status);
  * factors, 32..256, default 128); "panel_oz_min_rows" (in the emulated-FP64
  * and FP32 forms, panels with at least this many rows apply each half's Q^T to
  * the other half of the panel in emulated FP64 on the tensor cores instead of
- * the FP64 pipe; default 2048, 0 disables); "ls_refine" (candmc_ls_solve's refinement: 0, the
+ * the FP64 pipe; default 8192, 0 disables); "ls_refine" (candmc_ls_solve's refinement: 0, the
  * default, the corrected semi-normal equations; 1 the augmented system
  * [I A; A^T 0] refining x and r); "batched_form" (CANDMC_PREC_OZAKI, the
  * default: candmc_batched_ls's panels apply each half-panel's Q^T to the

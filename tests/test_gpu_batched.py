@@ -132,5 +132,5 @@ def test_batched_panel_forms(cm, form):
         torch.cuda.synchronize()
     finally:
         cm.set_tuning("batched_form", 1)
-        cm.set_tuning("panel_oz_min_rows", 2048)
+        cm.set_tuning("panel_oz_min_rows", 8192)
     check(host, xs)

@@ -151,7 +151,7 @@ def test_panel_split_update_on_tensor_cores(cm, m, k, b, min_rows):
             assert D.max() <= 1e-10 * np.abs(Ao).max(), D.max()
             assert co.backward_error(A, YR) <= BWD_TOL
     finally:
-        cm.set_tuning("panel_oz_min_rows", 2048)
+        cm.set_tuning("panel_oz_min_rows", 8192)
 
 
 def test_panel_split_update_knob_rejects_negative(cm):
