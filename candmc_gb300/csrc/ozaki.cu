@@ -109,6 +109,15 @@ __device__ __forceinline__ f2 df_from_double(double x) {
 __device__ __forceinline__ double df_to_double(f2 x) { return (double)x.h + (double)x.l; }
 
 // ------------------------------------------------------------------ slicing
+// 2^e for -126 <= e <= 127 (a normal float): x * pow2f(e) rounds once, as
+// ldexpf(x, e) does
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+
+// x * 2^k rounded once: one multiplication when 2^k is a normal float
+__device__ __forceinline__ float scale_pow2(float x, int k) {
+  return (k >= -126 && k <= 127) ? __fmul_rn(x, pow2f(k)) : ldexpf(x, k);
+}
+
 // Scale exponent of a group maximum: smallest e with max < 2^e (0 for 0).
 __device__ __forceinline__ int scale_exp(float mx) {
   if (!(mx > 0.0f)) return 0;
@@ -121,7 +130,7 @@ __device__ __forceinline__ int scale_exp(float mx) {
 template <int S>
 __device__ __forceinline__ void slice_value(f2 v, int e, __nv_bfloat16* out, int64_t plane,
                                             int64_t off) {
-  float p = ldexpf(v.h, 8 - e), q = ldexpf(v.l, 8 - e);
+  float p = scale_pow2(v.h, 8 - e), q = scale_pow2(v.l, 8 - e);
   float w = 1.0f;
 #pragma unroll
   for (int i = 0; i < S; ++i) {
@@ -234,8 +243,8 @@ __global__ void __launch_bounds__(256) k_slice_kcol8(SliceSrc src, int64_t k0, i
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const float2 t = tile[r][blk * 16 + khalf * 8 + k7 + i];
-      p[i] = ldexpf(t.x, 8 - e);
-      q[i] = ldexpf(t.y, 8 - e);
+      p[i] = scale_pow2(t.x, 8 - e);
+      q[i] = scale_pow2(t.y, 8 - e);
     }
     const int64_t base = ((kb0 >> 4) + blk) * (Rpad * 16) + (n0 >> 3) * 128 + 4 * u;
     float w = 1.0f;
@@ -341,10 +350,6 @@ constexpr int OZ_EPI_COLS = OZ_N * 4 / OZ_EPI_WARPS;  // accumulator columns per
 constexpr int OZ_WARPS = 2 + OZ_EPI_WARPS;             // producer, MMA issuer, epilogue
 constexpr int OZ_THREADS = OZ_WARPS * 32;
 static_assert(OZ_EPI_WARPS % 4 == 0 && OZ_EPI_COLS % 16 == 0, "epilogue split");
-
-// 2^e for -126 <= e <= 127 (a normal float): x * pow2f(e) rounds once, as
-// ldexpf(x, e) does
-__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
 
 // The five accumulators of one output element as one df64 value.  Groups 0..3
 // hold the diagonals i + j = g of the slice products, exact multiples of

@@ -291,12 +291,12 @@ int candmc_batched_ls(int64_t nprob, const int64_t* m, const int64_t* n, double*
 
 /* candmc_batched_ls_f32: the float32-input variant (no counterpart in the
  * reference): A_i (ld lda_i) and b_i are float32; they are widened into an
- * FP64 work area on the device (kept per device, grown on demand, released at
- * exit), solved by candmc_batched_ls in FP64, and x_i is rounded into the
- * first n_i entries of b_i (A_i is left as it was).  At most 65535 problems per
- * call.  The host waits for the previous call on this device to finish (the
- * work area is shared) and synchronises the stream once to upload the problem
- * tables. */
+ * FP64 work area on the device (one per device, grown on demand and held until
+ * the process exits), solved by candmc_batched_ls in FP64, and x_i is rounded
+ * into the first n_i entries of b_i (A_i is left as it was).  At most 65535
+ * problems per call.  Calls from several host threads run one at a time; the
+ * host waits for the previous call on this device to finish (the work area is
+ * shared) and synchronises the stream once to upload the problem tables. */
 int candmc_batched_ls_f32(int64_t nprob, const int64_t* m, const int64_t* n, float* const* A,
                           const int64_t* lda, float* const* B, int nstreams, int use_graph, void* stream);
 
