@@ -73,3 +73,25 @@ def test_yamamoto_argument_errors_without_gpu(built):
     # QR_Yamamoto_2D_2D: b not a multiple of b_sub, m < k
     assert lib.candmc_QR_Yamamoto_2D_2D(dummy, 10, 10, 8, 6, 4, 0, None, 0, None, 0, None, None, 0, None) == 1
     assert lib.candmc_QR_Yamamoto_2D_2D(dummy, 10, 6, 8, 4, 4, 0, None, 0, None, 0, None, None, 0, None) == 1
+
+
+def test_batched_argument_errors_without_gpu(built):
+    """The batched entry points (FP64 and float32 inputs) reject a bad
+    problem before any device call: n above 128, m below n, lda below m,
+    a null pointer, and a negative count."""
+    import ctypes
+    from candmc_gb300 import _abi
+    lib = _abi.load()
+    dummy = ctypes.c_void_p(16)   # never dereferenced: every call below fails validation first
+
+    def args(m, n, lda, ptr=dummy):
+        arr = lambda t, v: (t * 1)(v)
+        return (arr(ctypes.c_int64, m), arr(ctypes.c_int64, n), arr(ctypes.c_void_p, ptr),
+                arr(ctypes.c_int64, lda), arr(ctypes.c_void_p, dummy))
+
+    for fn in (lib.candmc_batched_ls, lib.candmc_batched_ls_f32):
+        for m, n, lda, ptr in [(200, 129, 200, dummy), (10, 20, 10, dummy), (200, 8, 100, dummy),
+                               (200, 8, 200, None)]:
+            pm, pn, pa, pl, pb = args(m, n, lda, ptr)
+            assert fn(1, pm, pn, pa, pl, pb, 4, 0, None) == 1, (fn, m, n, lda, ptr)
+        assert fn(-1, None, None, None, None, None, 4, 0, None) == 1
