@@ -160,6 +160,7 @@ __device__ __forceinline__ f2 src_at(const SliceSrc& s, int64_t r, int64_t c) {
   switch (s.mask) {
     case kUnitLower: x = (r > c + s.off) ? s.d[c * s.ld + r] : (r == c + s.off ? 1.0 : 0.0); break;
     case kUpper: x = (r <= c + s.off) ? s.d[c * s.ld + r] : 0.0; break;
+    case kLower: x = (r >= c + s.off) ? s.d[c * s.ld + r] : 0.0; break;
     default: x = s.d[c * s.ld + r];
   }
   return df_from_double(x);
@@ -318,6 +319,7 @@ struct OzArgs {
   int64_t Mvalid, Nvalid;
   int64_t fp64_rows;         // mode 1: rows < fp64_rows are written as FP64 (final)
   int c_fp64;                // mode 1: C is stored as FP64 (read and written in FP64)
+  int c_assign;              // mode 1 with c_fp64: C = product (C is not read)
   int* status;
   int64_t n_mt, n_nt, n_ks;  // work items: M tiles x N tiles x K splits
 };
@@ -730,13 +732,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
 #pragma unroll
               for (int j = 0; j < 16; ++j) {
                 const int64_t gn = it.n0 + part * OZ_EPI_COLS + c16 * 16 + j;
-                cd[j] = (gn < a.Nvalid) ? a.C64[gn * a.ldc + gm] : 0.0;
+                cd[j] = (gn < a.Nvalid && !a.c_assign) ? a.C64[gn * a.ldc + gm] : 0.0;
               }
 #pragma unroll
               for (int j = 0; j < 16; ++j) {
                 const int64_t gn = it.n0 + part * OZ_EPI_COLS + c16 * 16 + j;
                 if (gn >= a.Nvalid) continue;
-                a.C64[gn * a.ldc + gm] = cd[j] - df_to_double(acc[c16 * 16 + j]);
+                const double pv = df_to_double(acc[c16 * 16 + j]);
+                a.C64[gn * a.ldc + gm] = a.c_assign ? pv : cd[j] - pv;
               }
               continue;
             }
@@ -794,15 +797,28 @@ __global__ void k_from_df64(double* X, int64_t ld, int64_t m, int64_t n) {
   *p = (double)v.x + (double)v.y;
 }
 
-// Z (nb x n, FP64, ld nb) = sum over splits of the df64 partials [split][n][AR].
+// Z (nb x n, FP64, ld nb) = sum over splits of the df64 partials [split][n][AR],
+// added in split order.  Eight partials are loaded before they are added, so a
+// narrow update's many splits (up to one per 128 rows) cost a few memory
+// latencies per output instead of one per split.
 __global__ void k_oz_sum_partials(const float2* part, int nsplit, int64_t AR, int nb, int64_t n,
                                   double* Z) {
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (int64_t)nb * n) return;
   int64_t i = idx % nb, j = idx / nb;
+  const float2* p = part + j * AR + i;
+  const int64_t stride = n * AR;
   f2 s = {0.0f, 0.0f};
-  for (int sp = 0; sp < nsplit; ++sp) {
-    float2 v = part[(int64_t)sp * n * AR + j * AR + i];
+  int sp = 0;
+  for (; sp + 8 <= nsplit; sp += 8) {
+    float2 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = p[(int64_t)(sp + u) * stride];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s = df_add(s, {v[u].x, v[u].y});
+  }
+  for (; sp < nsplit; ++sp) {
+    const float2 v = p[(int64_t)sp * stride];
     s = df_add(s, {v.x, v.y});
   }
   Z[j * nb + i] = df_to_double(s);
@@ -935,6 +951,44 @@ static int oz_tn(const SliceSrc& ysrc, const SliceSrc& csrc, int64_t m, int nb, 
   return CANDMC_OK;
 }
 
+// Zt (nb x n, FP64, ld nb) = Top (nb x nb) * Z (nb x n, FP64, ld nb) with the
+// S-slice contraction: Top is the A operand (sliced from its stored matrix,
+// transposed or not), Z the B operand, and the MODE 1 epilogue stores the
+// product into Zt instead of subtracting it.
+template <int S>
+static int oz_top_times(MatRef Top, int nb, const double* Z, int64_t n, double* Zt, int* status,
+                        cudaStream_t s, int cls) {
+  const int64_t Kp = rup(nb, 16), BR = rup(n, OZ_N);
+  DevBuf ta, et, zb, ez;
+  CANDMC_RET(ta.alloc(sizeof(__nv_bfloat16) * S * OZ_M * Kp, s));
+  CANDMC_RET(et.alloc(sizeof(int) * OZ_M, s));
+  CANDMC_RET(zb.alloc(sizeof(__nv_bfloat16) * S * BR * Kp, s));
+  CANDMC_RET(ez.alloc(sizeof(int) * BR, s));
+  auto* tas = static_cast<__nv_bfloat16*>(ta.p);
+  auto* zbs = static_cast<__nv_bfloat16*>(zb.p);
+  const SliceSrc tsrc{Top.p, nullptr, Top.ld, Top.mask, Top.off};
+  // A operand element (i, k) = Top(i, k): X[k, i] of a transposed reference
+  // (a column of X per operand row), X[i, k] otherwise (a row of X)
+  if (Top.trans)
+    CANDMC_RET(launch_slice_kcol<S>(tsrc, 0, nb, nb, OZ_M, Kp, (int)Kp, tas, static_cast<int*>(et.p), s));
+  else
+    CANDMC_RET(launch_slice_krow<S>(tsrc, 0, nb, nb, OZ_M, Kp, tas, static_cast<int*>(et.p), s));
+  CANDMC_RET(launch_slice_kcol<S>(SliceSrc{Z, nullptr, nb, kDense, 0}, 0, nb, n, BR, Kp, (int)Kp, zbs,
+                                  static_cast<int*>(ez.p), s));
+  OzArgs g{};
+  g.As = tas; g.AR = OZ_M; g.Bs = zbs; g.BR = BR;
+  g.Kpad = Kp; g.k_per_cta = Kp; g.kgroup = Kp;
+  g.eA = static_cast<int*>(et.p); g.eB = static_cast<int*>(ez.p);
+  g.mode = 1; g.C = reinterpret_cast<float2*>(Zt); g.C64 = Zt; g.ldc = nb;
+  g.Mvalid = nb; g.Nvalid = n; g.fp64_rows = 0; g.status = status;
+  g.c_fp64 = 1; g.c_assign = 1;
+  return launch_oz<S>(g, 1, (unsigned)(BR / OZ_N), 1, cls, 2.0 * nb * nb * n, s);
+}
+
+// Width from which the operator product T^T Z of an update runs on the
+// tensor cores (below it, the FP64 small-matrix kernel is quicker).
+constexpr int64_t kOzTopMinCols = 1024;
+
 // The trailing update with S-slice contractions: C <- C - Y (Top (Y^T C)).
 // C (m x n, ld ldc) holds df64 pairs; rows < fp64_rows of C are written back
 // as FP64 (finished R rows).  With c_fp64, C is FP64 storage instead (read and
@@ -954,9 +1008,12 @@ static int apply_qt_slices(const double* Y, int64_t ldy, int ymask, int64_t m, i
   DevBuf z, zt;
   CANDMC_RET(z.alloc(sizeof(double) * nb * n, s));
   CANDMC_RET(oz_tn<S>(ysrc, csrc, m, nb, n, z.d(), status, s, cls_tn));
-  // ---- Z' = T^T * Z   (FP64, nb x n)
+  // ---- Z' = T^T * Z   (FP64 storage, nb x n)
   CANDMC_RET(zt.alloc(sizeof(double) * nb * n, s));
-  CANDMC_RET(small_gemm(nb, n, nb, 1.0, Top, mref(z.d(), nb), 0.0, zt.d(), nb, s));
+  if (n >= kOzTopMinCols)
+    CANDMC_RET(oz_top_times<S>(Top, nb, z.d(), n, zt.d(), status, s, cls_tn));
+  else
+    CANDMC_RET(small_gemm(nb, n, nb, 1.0, Top, mref(z.d(), nb), 0.0, zt.d(), nb, s));
   // ---- GEMM2: C -= Y * Z'.  A-op = Y (rows = m, K = nb), B-op = Z'^T (rows = columns, K = nb)
   const int64_t Kp2 = rup(nb, 16);
   const int64_t AR2 = rup(m, OZ_M), BR2 = rup(n, OZ_N);
