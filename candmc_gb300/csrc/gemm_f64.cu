@@ -86,6 +86,49 @@ k_gemm_f64(MatRef A, MatRef B, int64_t M, int64_t N, int64_t K, int64_t kchunk, 
   }
 }
 
+// Single-column forms (one right-hand side: Q^T b, Q b).  A 16 x 16 tile for
+// one column would spend 15 of every 16 DFMAs on padding, so these run one
+// FMA per element of Y, which is what bounds a matrix-vector product on the
+// FP64 pipe.
+//
+// part[z * nb + i] = sum over the rows r of chunk z of Y(r, i) * c(r): one warp
+// per column i of Y (lanes stride the rows, four accumulators), warp-reduced.
+__global__ void __launch_bounds__(kThreads)
+k_gemv_tn(MatRef Y, MatRef C, int64_t m, int nb, int64_t kchunk, double* part) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * (kThreads / 32) + warp;
+  if (i >= nb) return;   // warp-uniform
+  const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+  const int64_t k1 = (k0 + kchunk < m) ? k0 + kchunk : m;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  int64_t r = k0 + lane;
+  for (; r + 96 < k1; r += 128) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] = fma(mat_at(Y, r + 32 * u, i), mat_at(C, r + 32 * u, 0), acc[u]);
+  }
+  for (; r < k1; r += 32) acc[0] = fma(mat_at(Y, r, i), mat_at(C, r, 0), acc[0]);
+  const double sum = warp_sum((acc[0] + acc[1]) + (acc[2] + acc[3]));
+  if (lane == 0) part[(int64_t)blockIdx.y * nb + i] = sum;
+}
+
+// c(r) -= sum_k Y(r, k) z(k), one thread per row r (z staged in shared memory)
+__global__ void __launch_bounds__(kThreads)
+k_gemv_nn_sub(double* C, MatRef Y, const double* Z, int64_t m, int nb) {
+  __shared__ double sz[256];
+  for (int k = threadIdx.x; k < nb; k += kThreads) sz[k] = Z[k];
+  __syncthreads();
+  const int64_t r = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (r >= m) return;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  int k = 0;
+  for (; k + 4 <= nb; k += 4) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] = fma(mat_at(Y, r, k + u), sz[k + u], acc[u]);
+  }
+  for (; k < nb; ++k) acc[0] = fma(mat_at(Y, r, k), sz[k], acc[0]);
+  C[r] -= (acc[0] + acc[1]) + (acc[2] + acc[3]);
+}
+
 // Small-matrix product, 16 x 16 outputs per CTA, one per thread:
 // C(i,j) = alpha * sum_k opA(i,k) opB(k,j) + beta * C(i,j)   (beta == 0: C not read).
 __global__ void __launch_bounds__(kThreads)
@@ -283,6 +326,27 @@ int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top,
                    double* Z, int64_t ldz, cudaStream_t s) {
   if (nb <= 0 || n <= 0) return CANDMC_OK;
   if (nb > 256) return CANDMC_ERR_ARG;
+  if (n == 1) {
+    // one column: a warp per column of Y over row slices, about 8 CTAs per SM
+    const int64_t cblk = (nb + kThreads / 32 - 1) / (kThreads / 32);
+    int64_t nsplit = std::max<int64_t>(1, std::min<int64_t>((8 * (int64_t)num_sms() + cblk - 1) / cblk,
+                                                            (m + 255) / 256));
+    int64_t kchunk = (m + nsplit - 1) / nsplit;
+    nsplit = std::max<int64_t>(1, (m + kchunk - 1) / kchunk);
+    DevBuf part;
+    CANDMC_RET(part.alloc(sizeof(double) * (size_t)nb * nsplit, s));
+    {
+      ProfScope ps(CANDMC_KCLASS_GEMM_TN, 2.0 * nb * m, s);
+      k_gemv_tn<<<dim3((unsigned)cblk, (unsigned)nsplit), kThreads, 0, s>>>(Y, C, m, nb, kchunk, part.d());
+    }
+    CANDMC_CK(cudaGetLastError());
+    int nbp = 1;
+    while (nbp < nb) nbp <<= 1;
+    ProfScope ps(CANDMC_KCLASS_REDUCE, 8.0 * nb * nsplit, s);
+    k_reduce_apply<<<1u, kThreads, 0, s>>>(part.d(), (int)nsplit, nb, nb, nbp, 1, Top, alpha, Z, ldz);
+    CANDMC_CK(cudaGetLastError());
+    return CANDMC_OK;
+  }
   // the widest tile that, split over 64-row slices, still fills the GPU; for
   // narrow products 16 x 16 tiles over slices down to TK rows
   const int U = tile_u(nb, n, std::max<int64_t>(1, m / 64));
@@ -323,6 +387,12 @@ int gemm_tn_reduce(MatRef Y, MatRef C, int64_t m, int nb, int64_t n, MatRef Top,
 int gemm_nn_sub(double* C, int64_t ldc, MatRef Y, const double* Z, int64_t ldz, int64_t m, int64_t n,
                 int nb, cudaStream_t s) {
   if (m <= 0 || n <= 0 || nb <= 0) return CANDMC_OK;
+  if (n == 1 && nb <= 256) {
+    ProfScope ps(CANDMC_KCLASS_GEMM_NN, 2.0 * m * nb, s);
+    k_gemv_nn_sub<<<(unsigned)((m + kThreads - 1) / kThreads), kThreads, 0, s>>>(C, Y, Z, m, nb);
+    CANDMC_CK(cudaGetLastError());
+    return CANDMC_OK;
+  }
   const int U = tile_u(m, n, 1);
   const int T = 16 * U;
   dim3 grid((unsigned)((m + T - 1) / T), (unsigned)((n + T - 1) / T), 1);

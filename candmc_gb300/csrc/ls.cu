@@ -86,6 +86,55 @@ __global__ void __launch_bounds__(256) k_ts_gemm(const double* A, int64_t lda, c
   }
 }
 
+// One right-hand side: a 16-column tile would spend 15 of every 16 DFMAs on
+// padding, so r = 1 runs one FMA per element of A (the FP64 pipe's bound for
+// a matrix-vector product).
+// part[z * M + i] = sum over k in chunk z of A[k * lda + i] * x[k]   (A x, A: M x K)
+__global__ void __launch_bounds__(256) k_gemv_n(const double* A, int64_t lda, const double* x, int64_t M,
+                                                int64_t K, int64_t kchunk, double* part) {
+  __shared__ double sx[256];
+  const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+  const int64_t k1 = (k0 + kchunk < K) ? k0 + kchunk : K;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int64_t kb = k0; kb < k1; kb += 256) {
+    const int kn = (int)((k1 - kb < 256) ? k1 - kb : 256);
+    __syncthreads();
+    if (threadIdx.x < kn) sx[threadIdx.x] = x[kb + threadIdx.x];
+    __syncthreads();
+    if (i < M) {
+      int k = 0;
+      for (; k + 4 <= kn; k += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[u] = fma(A[(kb + k + u) * lda + i], sx[k + u], acc[u]);
+      }
+      for (; k < kn; ++k) acc[0] = fma(A[(kb + k) * lda + i], sx[k], acc[0]);
+    }
+  }
+  if (i < M) part[(int64_t)blockIdx.y * M + i] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+}
+
+// part[z * M + j] = sum over k in chunk z of A[j * lda + k] * x[k]   (A^T x, A: K x M):
+// one warp per column j, lanes stride the rows
+__global__ void __launch_bounds__(256) k_gemv_t(const double* A, int64_t lda, const double* x, int64_t M,
+                                                int64_t K, int64_t kchunk, double* part) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t j = (int64_t)blockIdx.x * 8 + warp;
+  if (j >= M) return;   // warp-uniform
+  const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+  const int64_t k1 = (k0 + kchunk < K) ? k0 + kchunk : K;
+  const double* a = A + j * lda;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  int64_t k = k0 + lane;
+  for (; k + 96 < k1; k += 128) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] = fma(a[k + 32 * u], x[k + 32 * u], acc[u]);
+  }
+  for (; k < k1; k += 32) acc[0] = fma(a[k], x[k], acc[0]);
+  const double sum = warp_sum((acc[0] + acc[1]) + (acc[2] + acc[3]));
+  if (lane == 0) part[(int64_t)blockIdx.y * M + j] = sum;
+}
+
 // out (M x r, ld ldo) = beta * Cin + alpha * sum_z part[z]
 __global__ void k_ts_reduce(const double* part, int nsplit, int64_t M, int64_t r, double alpha,
                             double beta, const double* Cin, int64_t ldc, double* out, int64_t ldo) {
@@ -174,6 +223,30 @@ static int ts_gemm(bool trans, const double* A, int64_t lda, const double* X, in
                    int64_t K, int64_t r, double alpha, double beta, const double* Cin, int64_t ldc,
                    double* out, int64_t ldo, cudaStream_t s) {
   if (M <= 0 || r <= 0) return CANDMC_OK;
+  if (r == 1 && K > 0) {
+    // about 8 CTAs per SM: row (or column) blocks times K chunks
+    const int64_t blk = trans ? (M + 7) / 8 : (M + 255) / 256;
+    int64_t nsplit = std::max<int64_t>(1, std::min<int64_t>((8 * ls_sms() + blk - 1) / blk,
+                                                            (K + 255) / 256));
+    int64_t kchunk = (K + nsplit - 1) / nsplit;
+    nsplit = std::max<int64_t>(1, (K + kchunk - 1) / kchunk);
+    DevBuf part;
+    CANDMC_RET(part.alloc(sizeof(double) * nsplit * M, s));
+    {
+      ProfScope ps(CANDMC_KCLASS_GEMM_TN, 2.0 * M * K, s);
+      const dim3 g((unsigned)blk, (unsigned)nsplit);
+      if (trans)
+        k_gemv_t<<<g, 256, 0, s>>>(A, lda, X, M, K, kchunk, part.d());
+      else
+        k_gemv_n<<<g, 256, 0, s>>>(A, lda, X, M, K, kchunk, part.d());
+      CANDMC_CK(cudaGetLastError());
+    }
+    ProfScope ps(CANDMC_KCLASS_REDUCE, 8.0 * nsplit * M, s);
+    k_ts_reduce<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(part.d(), (int)nsplit, M, 1, alpha, beta, Cin, ldc,
+                                                            out, ldo);
+    CANDMC_CK(cudaGetLastError());
+    return CANDMC_OK;
+  }
   const int64_t tiles = ((M + TS_M - 1) / TS_M) * ((r + TS_R - 1) / TS_R);
   int64_t nsplit = std::max<int64_t>(1, std::min<int64_t>((4 * ls_sms() + tiles - 1) / tiles, (K + 127) / 128));
   int64_t kchunk = ((K + nsplit - 1) / nsplit + TS_K - 1) / TS_K * TS_K;
