@@ -103,6 +103,9 @@ __device__ __forceinline__ double nr_rsqrt(double q) {
 // the reconstruction, so that the T^-1 identity holds for every reflector.
 constexpr int kLeafThreads = 128;   // 4 warps, one per SMSP
 constexpr int kMaxR = 8;            // rows per lane: leaves of up to 256 rows, nodes of 4 x 32
+// leaves from which the Y formation takes its path products from a top-down
+// pass over the nodes instead of multiplying each leaf's whole path itself
+constexpr int kNodeMinLeaves = 256;
 
 // Sum over the warp of eight values per lane; every lane receives all eight sums.
 __device__ __forceinline__ void warp_sum8(const double (&d)[8], double (&out)[8]) {
@@ -479,6 +482,8 @@ struct Hr4Args {
   unsigned* ticket; // pipelined tree: role counter
   int* fail;        // pipelined tree: a wait gave up
   double* Pc;       // pipelined tree: prefix products of Q1_top along leaf 0's path, (depth + 1) x b x b
+  double* Mn;       // many leaves: per node, the product of the Q blocks from the root down to it
+                    // times U^-1 (nnodes x b x b, by flat id), or nullptr
   int P;
   int ldS;          // leading dimension of the shared block (>= 32 * ceil(leaf rows / 32), >= 128)
   int depth;
@@ -1034,6 +1039,33 @@ __global__ void __launch_bounds__(kLeafThreads) k_hr6_pipe(Hr4Args a) {
     h6_root_solver(a, sm6, &s_ok);
 }
 
+// The product of the Q blocks along the root-to-node path times U^-1, for
+// every node of level lvl (1 <= lvl < depth), from the parents' products:
+// M(node) = Q(parent, child index) M(parent), or M(parent) for an only child,
+// with M(root) = U^-1.  Run level by level from the top, this forms every
+// path product once (about P / 3 products) instead of once per leaf and
+// level (P x depth) in k_hr4_form_y.
+__global__ void __launch_bounds__(kLeafThreads) k_hr4_node_m(Hr4Args a, int lvl) {
+  extern __shared__ double sm4[];
+  const int b = a.b, tid = threadIdx.x;
+  const int c = blockIdx.x;                 // node index within level lvl
+  const int nd = c / kFan;                  // parent at level lvl + 1
+  const size_t nb2 = (size_t)b * b;
+  const double* Mp = (lvl + 1 == a.depth) ? a.Uinv : a.Mn + (size_t)(a.base[lvl + 1] + nd) * nb2;
+  double* Mo = a.Mn + (size_t)(a.base[lvl] + c) * nb2;
+  double* sQ = sm4;
+  double* sM = sQ + nb2;
+  double* sO = sM + nb2;
+  if (h4_children(a, lvl + 1, nd) > 1) {
+    h4_load(sQ, a.Qn + ((size_t)(a.base[lvl + 1] + nd) * kFan + (c - nd * kFan)) * nb2, b);
+    h4_load(sM, Mp, b);
+    h5_mm(sQ, b, false, kSUpper, sM, b, false, kSUpper, sO, b, b, 1.0, nullptr);
+    for (int idx = tid; idx < b * b; idx += blockDim.x) Mo[idx] = sO[idx];
+  } else {
+    for (int idx = tid; idx < b * b; idx += blockDim.x) Mo[idx] = __ldcg(Mp + idx);
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
   extern __shared__ double sm4[];
   const int b = a.b, tid = threadIdx.x;
@@ -1044,8 +1076,13 @@ __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
   double* sX = sM + b * b;
   double* sY = sX + b * b;
   double* sT = sY + b * b;
-  h4_load(sM, a.Uinv, b);
-  for (int lvl = a.depth; lvl >= 1; --lvl) {
+  // the levels above 1 come from k_hr4_node_m when it ran (a.Mn)
+  const int top = (a.Mn && a.depth >= 2) ? 1 : a.depth;
+  if (top < a.depth)
+    h4_load(sM, a.Mn + (size_t)(a.base[1] + leaf / kFan) * b * b, b);
+  else
+    h4_load(sM, a.Uinv, b);
+  for (int lvl = top; lvl >= 1; --lvl) {
     int nd = leaf;
     for (int l = 0; l < lvl; ++l) nd /= kFan;
     int child = leaf;
@@ -1151,7 +1188,10 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   const size_t o_qn = o_tl + rup256(sizeof(double) * nb2 * P);
   const size_t o_uinv = o_qn + rup256(sizeof(double) * nb2 * kFan * nnodes);
   const size_t o_pc = o_uinv + rup256(sizeof(double) * nb2);
-  const size_t total_bytes = o_pc + (pipe ? rup256(sizeof(double) * nb2 * (a.depth + 1)) : 0);
+  // many leaves: the path products are formed once per node, top down
+  const bool node_m = P >= kNodeMinLeaves && a.depth >= 2;
+  const size_t o_mn = o_pc + (pipe ? rup256(sizeof(double) * nb2 * (a.depth + 1)) : 0);
+  const size_t total_bytes = o_mn + (node_m ? rup256(sizeof(double) * nb2 * nnodes) : 0);
   DevBuf ws;
   CANDMC_RET(ws.alloc(total_bytes, s));
   char* base = static_cast<char*>(ws.p);
@@ -1171,6 +1211,7 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
   }
   a.T = T; a.ldT = ldT; a.W = W; a.ldW = ldW;
   a.Uinv = reinterpret_cast<double*>(base + o_uinv);
+  a.Mn = node_m ? reinterpret_cast<double*>(base + o_mn) : nullptr;
   a.status = d_status;
   static std::atomic<bool> attr{false};
   if (!attr) {
@@ -1187,6 +1228,13 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
       k_hr4_leaf_tree<<<(unsigned)P, kLeafThreads, sm, s>>>(a);
   }
   CANDMC_CK(cudaGetLastError());
+  if (node_m) {
+    for (int lvl = a.depth - 1; lvl >= 1; --lvl) {
+      ProfScope ps(CANDMC_KCLASS_PANEL_Y, 2.0 * a.nlev[lvl] * (double)nb2 * b / 3.0, s);
+      k_hr4_node_m<<<(unsigned)a.nlev[lvl], kLeafThreads, sizeof(double) * 3 * nb2, s>>>(a, lvl);
+      CANDMC_CK(cudaGetLastError());
+    }
+  }
   {
     ProfScope ps(CANDMC_KCLASS_PANEL_Y, 2.0 * m * b * b, s);
     k_hr4_form_y<<<(unsigned)P, kThreads, sizeof(double) * 4 * nb2, s>>>(a);

@@ -83,6 +83,29 @@ def test_hh_recon_vs_oracle(cm, m, b):
     assert co.backward_error(A, YR) <= BWD_TOL
 
 
+@pytest.mark.parametrize("m,b,pipe", [(300000, 32, 1), (70000, 32, 0), (40000, 24, 1)])
+def test_hh_recon_many_leaves(cm, m, b, pipe):
+    """Panels with hundreds to thousands of leaves: the Y formation takes each
+    leaf's path product from the top-down pass over the tree nodes.  Covers the
+    level-by-level tree (more than 4096 tree CTAs, or pipe_tree 0) and the
+    pipelined one; same bars as test_hh_recon_vs_oracle."""
+    A = fx.gaussian(m, b, 7 * m + b)
+    YRo, Wo = co.hh_recon_qr(A, b)
+    dA = dev(A)
+    try:
+        cm.set_tuning("pipe_tree", pipe)
+        W, T = cm.hh_recon_qr(dA)
+        torch.cuda.synchronize()
+    finally:
+        cm.set_tuning("pipe_tree", 1)
+    YR = host(dA)
+    assert np.abs(YR - YRo).max() <= tol(b, np.abs(YRo).max())
+    assert np.abs(host(W) - Wo).max() <= tol(b)
+    To = co.T_from_W(Wo, lp.unit_lower(YRo, b)[:b])
+    assert np.abs(host(T) - To).max() <= tol(b)
+    assert co.backward_error(A, YR) <= BWD_TOL
+
+
 @pytest.mark.parametrize("m,b", [(34, 17), (68, 17), (136, 17), (42, 21), (8 * 21, 21)])
 def test_hh_recon_reference_fixture(cm, m, b):
     """The reference test's own fixture and pass criterion (test_hh_recon.cxx)."""
