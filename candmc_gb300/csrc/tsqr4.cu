@@ -106,6 +106,8 @@ constexpr int kMaxR = 8;            // rows per lane: leaves of up to 256 rows, 
 // leaves from which the Y formation takes its path products from a top-down
 // pass over the nodes instead of multiplying each leaf's whole path itself
 constexpr int kNodeMinLeaves = 256;
+// rows from which the lookahead's panels take 256-row leaves
+constexpr int64_t kTallPanelRows = 32768;
 
 // Sum over the warp of eight values per lane; every lane receives all eight sums.
 __device__ __forceinline__ void warp_sum8(const double (&d)[8], double (&out)[8]) {
@@ -1139,7 +1141,10 @@ __global__ void __launch_bounds__(kThreads) k_hr4_form_y(Hr4Args a) {
 int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT, double* W,
                int64_t ldW, int* d_status, cudaStream_t s) {
   if (b < 1 || b > kDirectB || m < b) return CANDMC_ERR_ARG;
-  const int64_t want = t_leaf_rows > 0 ? t_leaf_rows : g_leaf_rows;
+  int64_t want = t_leaf_rows > 0 ? t_leaf_rows : g_leaf_rows;
+  // the lookahead's tall panels (thousands of leaves: throughput, not the
+  // latency of one leaf, sets the time) take 256-row leaves
+  if (t_leaf_rows > 0 && m >= kTallPanelRows) want = std::max<int64_t>(want, 256);
   const int64_t leaf_rows = std::max<int64_t>(32, std::min<int64_t>(want, 256));
   // leaves of at most leaf_rows rows and at least b rows
   int64_t P = std::max<int64_t>(1, std::min<int64_t>((m + leaf_rows - 1) / leaf_rows, m / b));
@@ -1236,8 +1241,12 @@ int hr_direct4(double* A, int64_t lda, int64_t m, int b, double* T, int64_t ldT,
     }
   }
   {
+    // with several waves of leaves, one thread per leaf row: leaves of at most
+    // 128 rows take 128-thread CTAs, so two of them (252 registers a thread)
+    // share an SM; a single wave keeps 256 threads for the path products
+    const unsigned ythreads = (Lmax <= 128 && P >= kNodeMinLeaves) ? 128u : (unsigned)kThreads;
     ProfScope ps(CANDMC_KCLASS_PANEL_Y, 2.0 * m * b * b, s);
-    k_hr4_form_y<<<(unsigned)P, kThreads, sizeof(double) * 4 * nb2, s>>>(a);
+    k_hr4_form_y<<<(unsigned)P, ythreads, sizeof(double) * 4 * nb2, s>>>(a);
   }
   CANDMC_CK(cudaGetLastError());
   return CANDMC_OK;

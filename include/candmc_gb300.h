@@ -312,7 +312,8 @@ int candmc_batched_status(void* stream, int* status);
  * column; 0: level by level); "oz_reserve_sms" (SMs kept free of the
  * persistent emulated-FP64 update kernel during QR_2D_pipe, for the panel
  * stream; default 32); "pipe_leaf_rows" (leaf height of the panels QR_2D_pipe
- * factors, 32..256, default 128); "panel_oz_min_rows" (in the emulated-FP64
+ * factors, 32..256, default 128; panels of 32768 rows or more take at least
+ * 256); "panel_oz_min_rows" (in the emulated-FP64
  * and FP32 forms, panels with at least this many rows apply each half's Q^T to
  * the other half of the panel in emulated FP64 on the tensor cores instead of
  * the FP64 pipe; default 8192, 0 disables); "ls_refine" (candmc_ls_solve's refinement: 0, the
