@@ -95,3 +95,27 @@ def test_batched_argument_errors_without_gpu(built):
             pm, pn, pa, pl, pb = args(m, n, lda, ptr)
             assert fn(1, pm, pn, pa, pl, pb, 4, 0, None) == 1, (fn, m, n, lda, ptr)
         assert fn(-1, None, None, None, None, None, 4, 0, None) == 1
+
+
+def test_tuning_knobs_without_gpu(built):
+    """Every tuning knob the header documents is accepted in range and rejected
+    out of range (host state only; the defaults are put back)."""
+    import re
+    from candmc_gb300 import _abi
+    lib = _abi.load()
+    header = open(os.path.join(ROOT, "include", "candmc_gb300.h")).read()
+    cases = {   # knob: (default, a valid value, an invalid value)
+        "leaf_rows": (64, 128, 16),
+        "oz_reserve_sms": (32, 24, -1),
+        "pipe_leaf_rows": (128, 256, 512),
+        "batched_form": (1, 0, 2),
+        "ls_refine": (0, 1, 3),
+        "panel_oz_min_rows": (8192, 0, -5),
+        "pipe_tree": (1, 0, 2),
+    }
+    for key, (default, ok, bad) in cases.items():
+        assert re.search(r'"%s"' % key, header), key          # documented
+        assert lib.candmc_set_tuning(key.encode(), ok) == 0, key
+        assert lib.candmc_set_tuning(key.encode(), bad) == 1, key
+        assert lib.candmc_set_tuning(key.encode(), default) == 0, key
+    assert lib.candmc_set_tuning(b"no_such_knob", 1) == 1
