@@ -550,6 +550,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
                  "r"(512));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  // An A operand of fewer than 128 rows (a narrow Y^T, stored with AR rows)
+  // fills only the first AR x 32 bytes of each slice block; the rest of every
+  // stage's A blocks is zeroed once here and never written again, so the
+  // 128-row MMA reads zeros there.
+  if (MODE == 0 && a.AR < OZ_M) {
+    const int abytes = (int)a.AR * 32;
+    const int tail = (OZ_ABYTES - abytes) / 16;
+    for (int idx = tid; idx < OZ_STAGES * S * tail; idx += blockDim.x) {
+      const int blk = idx / tail, q = idx % tail;
+      *reinterpret_cast<uint4*>(ring + (size_t)(blk / S) * STAGE_BYTES + (size_t)(blk % S) * OZ_ABYTES + abytes +
+                                16 * q) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -565,13 +579,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(OzArgs a) {
         for (int64_t kb = it.kbeg >> 4; kb < (it.kend >> 4); ++kb, ++gs) {
           const int st = (int)(gs % OZ_STAGES);
           if (!oz_wait(&empty_b[st], (uint32_t)(((gs / OZ_STAGES) & 1) ^ 1), &s_fail)) break;
-          mbar_expect_tx(&full_b[st], (unsigned)STAGE_BYTES);
+          const int abytes = (MODE == 0 && a.AR < OZ_M) ? (int)a.AR * 32 : OZ_ABYTES;
+          mbar_expect_tx(&full_b[st], (unsigned)(S * (abytes + OZ_BBYTES)));
           unsigned char* sb = ring + (size_t)st * STAGE_BYTES;
 #pragma unroll 1
           for (int sl = 0; sl < S; ++sl) {
             bulk_g2s(smem_u32(sb + sl * OZ_ABYTES),
                      a.As + (int64_t)sl * a.AR * a.Kpad + kb * a.AR * 16 + (it.m0 >> 3) * 128,
-                     (unsigned)OZ_ABYTES, &full_b[st]);
+                     (unsigned)abytes, &full_b[st]);
             bulk_g2s(smem_u32(sb + S * OZ_ABYTES + sl * OZ_BBYTES),
                      a.Bs + (int64_t)sl * a.BR * a.Kpad + kb * a.BR * 16 + (it.n0 >> 3) * 128,
                      (unsigned)OZ_BBYTES, &full_b[st]);
@@ -922,7 +937,9 @@ static int oz_tn(const SliceSrc& ysrc, const SliceSrc& csrc, int64_t m, int nb, 
   const int64_t KG = 128;                       // K rows per exact accumulation
   // A-op = Y^T (rows = Householder index, K = m), B-op = C (rows = columns)
   const int64_t Kp1 = rup(m, KG);
-  const int64_t AR1 = OZ_M, BR1 = rup(n, OZ_N);
+  // the A operand keeps only its nb rows (rounded to a core matrix of 8):
+  // the kernel zero-fills the rest of the 128-row tile in shared memory
+  const int64_t AR1 = rup(nb, 8), BR1 = rup(n, OZ_N);
   DevBuf ya, ea, cb, eb, part;
   CANDMC_RET(ya.alloc(sizeof(__nv_bfloat16) * S * AR1 * Kp1, s));
   CANDMC_RET(ea.alloc(sizeof(int) * (Kp1 / KG) * AR1, s));
