@@ -592,7 +592,8 @@ def wl_caqr(args, ctx):
                 "frac": achieved / pk if achieved else None,
                 "bf16_issued_tflops": achieved * 28.0 if achieved else None,
                 "traffic": traffic_from_profile("ozaki_gemm_caqr_n16384.md"),
-                "kernel": "k_oz_mma (Ozaki BF16 slice contractions on tcgen05, Y^T A and A -= Y Z)",
+                "kernel": "k_oz_mma (Ozaki BF16 slice contractions on tcgen05, Y^T A and A -= Y Z; "
+                          "the b x b operator product T^T Z is counted under 'small')",
                 "launches": dom_l, "share_of_step": dom_ms / t_max if t_max else None,
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained / 28 slice products "
                                "(of measured)"}

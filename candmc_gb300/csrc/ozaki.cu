@@ -1025,10 +1025,11 @@ static int apply_qt_slices(const double* Y, int64_t ldy, int ymask, int64_t m, i
   DevBuf z, zt;
   CANDMC_RET(z.alloc(sizeof(double) * nb * n, s));
   CANDMC_RET(oz_tn<S>(ysrc, csrc, m, nb, n, z.d(), status, s, cls_tn));
-  // ---- Z' = T^T * Z   (FP64 storage, nb x n)
+  // ---- Z' = T^T * Z   (FP64 storage, nb x n); counted, as on the FP64 pipe,
+  // under the small-product class, apart from the two contractions with Y
   CANDMC_RET(zt.alloc(sizeof(double) * nb * n, s));
   if (n >= kOzTopMinCols)
-    CANDMC_RET(oz_top_times<S>(Top, nb, z.d(), n, zt.d(), status, s, cls_tn));
+    CANDMC_RET(oz_top_times<S>(Top, nb, z.d(), n, zt.d(), status, s, CANDMC_KCLASS_SMALL));
   else
     CANDMC_RET(small_gemm(nb, n, nb, 1.0, Top, mref(z.d(), nb), 0.0, zt.d(), nb, s));
   // ---- GEMM2: C -= Y * Z'.  A-op = Y (rows = m, K = nb), B-op = Z'^T (rows = columns, K = nb)
