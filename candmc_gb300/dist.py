@@ -157,6 +157,28 @@ def sharded_hh_recon(A_local, b, kernels, group=None, root=0):
     return Y, Rout, W * signs[None, :]
 
 
+def sharded_lstsq(A_local, b_local, kernels, group=None, root=0):
+    """min ||A x - b|| for A (m x n) and b (m) split by rows over the ranks
+    of `group`: the TSQR of [A | b] (n + 1 columns) up the reference's tree
+    (sharded_tsqr) leaves R_aug = [[R, z], [0, rho]] on the root, with
+    z = (Q^T b)[:n] and |rho| = ||b - A x||; the root solves R x = z and
+    broadcasts x and |rho|.  Q is never formed.  Every rank needs at least
+    n + 1 rows.  Returns (x, residual norm) on every rank."""
+    import torch.distributed as dist
+    rank, p = dist.get_rank(group), dist.get_world_size(group)
+    myr = (rank - root) % p
+    n = A_local.shape[1]
+    Ab = torch.cat([A_local, b_local.reshape(-1, 1).to(A_local.dtype)], dim=1)
+    _, R = sharded_tsqr(Ab, n + 1, kernels, group, root)
+    out = torch.empty(n + 1, dtype=A_local.dtype, device=A_local.device)
+    if myr == 0:
+        x = torch.linalg.solve_triangular(R[:n, :n], R[:n, n:n + 1], upper=True)[:, 0]
+        out[:n] = x
+        out[n] = R[n, n].abs()
+    dist.broadcast(out, _global(root, group), group=group)
+    return out[:n].clone(), float(out[n])
+
+
 def column_block_update(Y, T, A_cols, kernels, group=None, panel_rank=0):
     """update_A over a process row (qr_2d.cxx:124-177): the rank that factored
     the panel broadcasts Y (unit-lower, explicit) and T (hh_recon's output

@@ -9,7 +9,10 @@ Checks, for 2 and 3 ranks and a rotated root:
   factorization of the whole panel (the reconstruction's output does not
   depend on the process count, hh_recon.cxx:129-321) -- within 1e-12;
 * the column-block update, with Y and T broadcast from the panel's rank,
-  equals upd_A on the whole matrix (qr_2d.cxx:124-177) -- within 1e-12.
+  equals upd_A on the whole matrix (qr_2d.cxx:124-177) -- within 1e-12;
+* the sharded least-squares solve (the TSQR of [A | b] up the same tree)
+  matches LAPACK's lstsq on the whole system -- within 1e-12, with the
+  residual norm.
 The ranks are separate processes (spawned) talking to each other only through
 torch.distributed on 127.0.0.1.  Not measured on GPUs: every box of this
 build has one GPU.
@@ -155,3 +158,34 @@ def test_sharded_hh_recon_and_update(world, m, b, root):
     for r in range(world):
         cols = out[r]["cols"]
         assert np.abs(out[r]["C"] - want[:, cols]).max() <= 1e-12 * max(1.0, np.abs(want).max())
+
+
+def _ls_worker(rank, world, port, m, n, root, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        A = fx.gaussian(m, n, 11 * m + n)
+        bvec = fx.gaussian(m, 1, 13 * m + n)[:, 0]
+        rows = np.array_split(np.arange(m), world)
+        myr = (rank - root) % world
+        x, rho = cdist.sharded_lstsq(torch.from_numpy(np.ascontiguousarray(A[rows[myr]])),
+                                     torch.from_numpy(np.ascontiguousarray(bvec[rows[myr]])),
+                                     OracleKernels(), root=root)
+        out[rank] = {"x": x.numpy(), "rho": rho}
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world,m,n,root", [(2, 300, 12, 0), (3, 400, 20, 1)])
+def test_sharded_lstsq(world, m, n, root):
+    mgr = mp.get_context("spawn").Manager()
+    out = mgr.dict()
+    mp.start_processes(_ls_worker, args=(world, _port(), m, n, root, out), nprocs=world, join=True,
+                       start_method="spawn")
+    A = fx.gaussian(m, n, 11 * m + n)
+    bvec = fx.gaussian(m, 1, 13 * m + n)[:, 0]
+    xo, res, _, _ = np.linalg.lstsq(A, bvec, rcond=None)
+    for r in range(world):
+        x = out[r]["x"]
+        assert np.linalg.norm(x - xo) <= 1e-12 * np.linalg.norm(xo)
+        assert abs(out[r]["rho"] - np.linalg.norm(bvec - A @ xo)) <= 1e-12 * np.linalg.norm(bvec)
